@@ -1,0 +1,257 @@
+/*
+ * dtrt_gb300 — C ABI of the GB300 differentiable volumetric path tracer.
+ *
+ * This is the boundary a host binding (ctypes, pybind11, cgo, JNI …) calls.
+ * Signatures carry plain pointers and sizes only; no C++ or torch types.
+ *
+ * The entry points replace, in the reference (uci-rendering/dtrt):
+ *   - the scene object graph built by the pybind constructors
+ *       src/dtrt.cpp:35-102 (Camera, Shape, BSDF_*, HG/Isotropic, AreaLight[Ex],
+ *       Homogeneous/Heterogeneous, Scene + initEdges) and Scene::Scene
+ *       src/scene.cpp:9-136;
+ *   - VolPathTracerAD::render, i.e. IntegratorAD::render
+ *       src/integrator/differential/integratorAD.cpp:19-166, bound at
+ *       src/dtrt.cpp:148-150;
+ *   - RenderOptions, include/integrator.h:10-25 and src/dtrt.cpp:104-115.
+ *
+ * Error convention: every entry point returns an int status (DTRT_OK == 0).
+ * On failure dtrt_last_error() returns a thread-local message. Nothing aborts
+ * the caller's process (the reference asserts, src/scene.cpp:568 et al.).
+ *
+ * Ownership: every pointer in a description is borrowed for the duration of
+ * the call only; dtrt_scene_create copies what it needs to the device
+ * (the reference copies at construction: src/shape.cpp:14-31,
+ * src/camera.cpp:13-27).
+ */
+#ifndef DTRT_GB300_H
+#define DTRT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DTRT_ABI_VERSION 1
+#define DTRT_MAX_NDER 8
+
+enum dtrt_status {
+    DTRT_OK = 0,
+    DTRT_ERR_INVALID = 1,     /* bad argument or scene description            */
+    DTRT_ERR_CUDA = 2,        /* a CUDA runtime call failed                    */
+    DTRT_ERR_OVERFLOW = 3,    /* a device work queue ran out of capacity       */
+    DTRT_ERR_UNSUPPORTED = 4, /* nder or feature not built                     */
+    DTRT_ERR_IO = 5,          /* volume file could not be read                 */
+    DTRT_ERR_STEP_CAP = 6,    /* a bounded device loop hit its iteration cap   */
+    DTRT_ERR_NO_DEVICE = 7    /* no CUDA device visible                        */
+};
+
+enum dtrt_bsdf_type { DTRT_BSDF_NULL = 0, DTRT_BSDF_DIFFUSE = 1, DTRT_BSDF_PHONG = 2, DTRT_BSDF_ROUGHDIELECTRIC = 3 };
+enum dtrt_phase_type { DTRT_PHASE_ISOTROPIC = 0, DTRT_PHASE_HG = 1 };
+enum dtrt_emitter_type { DTRT_EMITTER_AREA = 0, DTRT_EMITTER_AREA_EX = 1 };
+enum dtrt_medium_type { DTRT_MEDIUM_HOMOGENEOUS = 0, DTRT_MEDIUM_HETEROGENEOUS = 1 };
+
+/* EMode bitmask, include/integratorAD.h:12-24 */
+enum dtrt_mode {
+    DTRT_MODE_EMISSION = 0x01,
+    DTRT_MODE_SURFACE_MAIN = 0x02,
+    DTRT_MODE_SURFACE_BOUNDARY = 0x04,
+    DTRT_MODE_VOLUME_MAIN = 0x08,
+    DTRT_MODE_VOLUME_BOUNDARY1 = 0x10,
+    DTRT_MODE_VOLUME_BOUNDARY2 = 0x20,
+    DTRT_MODE_ALL = 0x3f
+};
+
+/* dtrt.Camera(w, h, c2w, c2ndc, clip_near, med_id, vel) + set_rect, src/camera.cpp:8-38 */
+typedef struct {
+    int width, height;
+    const float *cam_to_world; /* [16] row-major 4x4 */
+    const float *cam_to_ndc;   /* [9]  row-major 3x3 */
+    float clip_near;
+    int med_id;                /* -1: camera in vacuum */
+    const float *velocities;   /* NULL or [2*nder][3]: nder translations, then nder rotation axes */
+    int crop_offset_x, crop_offset_y, crop_width, crop_height; /* crop_width <= 0: full frame */
+} dtrt_camera_desc;
+
+/* dtrt.Shape(V, F, UV, N, nV, nT, light_id, bsdf_id, med_int, med_ext, vel), src/shape.cpp:10-52 */
+typedef struct {
+    const float *vertices;   /* [nv][3] */
+    const int *indices;      /* [nt][3] */
+    const float *uvs;        /* NULL or [nv][2] (accepted, unused by the shading model) */
+    const float *normals;    /* NULL or [nv][3] */
+    int num_vertices, num_triangles;
+    int light_id, bsdf_id, med_int_id, med_ext_id;
+    const float *velocities; /* NULL or [nder*nv][3]; with normals, followed by [nv][3] normal velocities */
+} dtrt_shape_desc;
+
+/* BSDF_null / BSDF_diffuse / BSDF_Phong / BSDF_roughdielectric, src/dtrt.cpp:55-67 */
+typedef struct {
+    int type;
+    float diffuse[3];        /* diffuse: reflectance; phong: diffuse reflectance */
+    float specular[3];       /* phong */
+    float exponent;          /* phong */
+    float alpha, int_ior, ext_ior; /* roughdielectric */
+    const float *d_diffuse;  /* NULL or [nder][3] */
+    const float *d_specular; /* NULL or [nder][3] */
+    const float *d_exponent; /* NULL or [nder] */
+    const float *d_alpha;    /* NULL or [nder] */
+    const float *d_eta;      /* NULL or [nder] */
+} dtrt_bsdf_desc;
+
+/* AreaLight(shape_id, I, two_sided) / AreaLightEx(shape_id, I, kappa[, dI, dK]), src/dtrt.cpp:76-81 */
+typedef struct {
+    int type;
+    int shape_id;
+    float intensity[3];
+    int two_sided;
+    float kappa;
+    const float *d_intensity; /* NULL or [nder][3] (AreaLightEx) */
+    const float *d_kappa;     /* NULL or [nder]    (AreaLightEx) */
+} dtrt_emitter_desc;
+
+/* HG(g[, dG]) / Isotropic(), src/dtrt.cpp:69-74 */
+typedef struct {
+    int type;
+    float g;
+    const float *d_g; /* NULL or [nder] */
+} dtrt_phase_desc;
+
+/* Homogeneous(...) / Heterogeneous(...), src/dtrt.cpp:83-93 */
+typedef struct {
+    int type;
+    int phase_id;
+    /* homogeneous */
+    float sigma_t;
+    float albedo[3];          /* also the constant albedo of a heterogeneous medium */
+    const float *d_sigma_t;   /* NULL or [nder] */
+    const float *d_albedo;    /* NULL or [nder][3] (both medium types) */
+    /* heterogeneous density grid: a Mitsuba VOL v3 file, or arrays when the file is NULL */
+    const char *density_file;
+    const float *density;     /* [res_z][res_y][res_x] */
+    int res[3];
+    float vol_min[3], vol_max[3];
+    /* optional 3-channel albedo grid (gridvolume albedo), same conventions */
+    const char *albedo_file;
+    const float *albedo_grid; /* [res_z][res_y][res_x][3] */
+    int albedo_res[3];
+    float albedo_min[3], albedo_max[3];
+    float to_world[16];       /* row-major 4x4 volume-to-world */
+    float density_scale;
+    const float *d_density_scale;  /* NULL or [nder] */
+    const float *trans_velocities; /* NULL or [nder][3] */
+    const float *rot_velocities;   /* NULL or [nder][3] */
+} dtrt_medium_desc;
+
+/* Scene(camera, shapes, bsdfs, emitters, phases, media) + initEdges(w), src/scene.cpp:9-142 */
+typedef struct {
+    int nder;                 /* derivative slots carried per path: 1, 3, 4 or 8 */
+    dtrt_camera_desc camera;
+    int num_shapes;   const dtrt_shape_desc *shapes;
+    int num_bsdfs;    const dtrt_bsdf_desc *bsdfs;
+    int num_emitters; const dtrt_emitter_desc *emitters;
+    int num_phases;   const dtrt_phase_desc *phases;
+    int num_media;    const dtrt_medium_desc *media;
+    const float *edge_weights; /* NULL or [num_shapes] secondary-edge sampling weights */
+} dtrt_scene_desc;
+
+/* RenderOptions(seed, spp, max_bounces, sppe, sppse, quiet[, mode[, ddistCoeff]]), include/integrator.h:10-25 */
+typedef struct {
+    uint64_t seed;
+    int spp;          /* num_samples */
+    int max_bounces;
+    int sppe;         /* num_samples_primary_edge */
+    int sppse;        /* num_samples_secondary_edge */
+    int quiet;
+    int mode;         /* < 0: all terms */
+    float ddist_coeff;
+} dtrt_render_options;
+
+/* Work counters and stage timings of the last render on a scene (device counters). */
+typedef struct {
+    uint64_t camera_paths;
+    uint64_t edge_records;    /* secondary-edge vertex records                      */
+    uint64_t edge_samples;    /* secondary-edge samples evaluated                   */
+    uint64_t lins_records;    /* Lins boundary records                              */
+    uint64_t primary_edge_samples;
+    uint64_t li_tasks;        /* non-AD sub-paths traced (edge, Lins, primary edge) */
+    uint64_t rays;            /* closest-hit queries                                */
+    uint64_t node_visits;     /* BVH nodes fetched                                  */
+    uint64_t tri_tests;       /* triangles fetched and tested                       */
+    uint64_t grid_lookups;    /* trilinear density lookups (8 voxels each)          */
+    uint64_t batches;         /* camera-path chunks the render was split into       */
+    double ms_total;
+    double ms_camera;         /* camera AD path kernel(s)                           */
+    double ms_edge;           /* secondary-edge kernel(s)                           */
+    double ms_li;             /* Li sub-path kernel(s)                              */
+    double ms_primary;        /* primary-edge kernel(s)                             */
+    double ms_setup;          /* scene upload / derived data for this render        */
+    int counters_enabled;
+} dtrt_render_stats;
+
+/* Opaque scene handle (device-resident geometry, BVH, media, edge tables). */
+typedef struct dtrt_scene dtrt_scene;
+
+/* ABI version of the loaded library (DTRT_ABI_VERSION). */
+int dtrt_abi_version(void);
+
+/* Number of visible CUDA devices (0 on a machine without a GPU). */
+int dtrt_device_count(void);
+
+/* Whether nder is one of the compiled derivative widths. Replaces the compile-time
+ * constant `nder` of include/config.h:5 (exported as dtrt.nder, src/dtrt.cpp:152). */
+int dtrt_nder_supported(int nder);
+
+/* Thread-local message for the last non-zero status. */
+const char *dtrt_last_error(void);
+
+/* Build a device scene: copies geometry and parameters, builds the BVH, light and
+ * edge distributions. Replaces Scene::Scene (src/scene.cpp:9-136) and the
+ * constructors it consumes. */
+int dtrt_scene_create(const dtrt_scene_desc *desc, dtrt_scene **out);
+
+/* Secondary-edge sampling weights per shape. Replaces Scene::initEdgesPy,
+ * include/scene.h:37-39 / src/scene.cpp:138-142. */
+int dtrt_scene_set_edge_weights(dtrt_scene *scene, const float *weights, int num_shapes);
+
+/* Release every device allocation of the scene. */
+int dtrt_scene_destroy(dtrt_scene *scene);
+
+/* Forward-mode render: image plus nder derivative images, float[(nder+1)][H][W][3]
+ * row-major (crop size when a crop rectangle is set). `out` is a host pointer when
+ * out_on_device == 0, else a device pointer. `stream` is a cudaStream_t or NULL.
+ * Primary-edge contributions are added to the derivative slots, matching
+ * IntegratorAD::render (integratorAD.cpp:19-166) as bound at src/dtrt.cpp:148-150.
+ * The call blocks until the result is written. */
+int dtrt_render_fwd(dtrt_scene *scene, const dtrt_render_options *opts, float *out,
+                    int out_on_device, void *stream);
+
+/* Enable (1) or disable (0) device work counters for later renders of a scene. */
+int dtrt_scene_enable_counters(dtrt_scene *scene, int enable);
+
+/* Counters and timings of the last render on the scene. */
+int dtrt_scene_last_stats(const dtrt_scene *scene, dtrt_render_stats *out);
+
+/* Maximum work-queue capacity in sub-path tasks (0 = automatic). Lets tests force
+ * a small queue; an overflow is reported as DTRT_ERR_OVERFLOW, never a hang. */
+int dtrt_scene_set_queue_capacity(dtrt_scene *scene, uint64_t max_tasks);
+
+/* Iteration cap of delta / ratio tracking loops (reference: 10000,
+ * src/medium/heterogeneous.cpp:6). A path that hits it is dropped and the render
+ * returns DTRT_ERR_STEP_CAP. */
+int dtrt_scene_set_tracking_cap(dtrt_scene *scene, int max_steps);
+
+/* Closest-hit queries against the scene BVH (device kernel), for tests of the
+ * traversal. rays: [n][8] = org.xyz, tmin, dir.xyz, tmax (host arrays).
+ * hits: [n][2] int = (global triangle id or -1, shape id); t: [n] float. */
+int dtrt_trace_closest(dtrt_scene *scene, const float *rays, int n, int *hits, float *t);
+
+/* Mitsuba VOL v3 grid reader (gridvolume.h:88-132). Pass data == NULL to query
+ * res/channels/bounds; then call again with data of res_x*res_y*res_z*channels floats. */
+int dtrt_vol_read(const char *path, int *res, int *channels, float *vmin, float *vmax, float *data);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DTRT_GB300_H */

@@ -1,0 +1,45 @@
+// dtrt_gb300 — host-side scene object and the per-width render entry points.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/dtrt_gb300.h"
+#include "dt_kernels.cuh"
+
+namespace dt {
+
+void set_last_error(const std::string &msg);
+
+// Device buffers reused across renders of one scene, grown on demand.
+struct Scratch {
+    double *acc1 = nullptr, *acc2 = nullptr;
+    size_t acc1_n = 0, acc2_n = 0;
+    float *out = nullptr;
+    size_t out_n = 0;
+    void *qe = nullptr, *ql = nullptr, *qli = nullptr;
+    size_t qe_bytes = 0, ql_bytes = 0, qli_bytes = 0;
+    unsigned long long *counts = nullptr;  // [0] edge recs, [1] lins recs, [2] li tasks, [8..] counters
+    unsigned int *err = nullptr;
+};
+
+}  // namespace dt
+
+struct dtrt_scene {
+    int nder = 0;
+    int device = 0;
+    dt::DevScene dev{};
+    std::vector<void *> allocs;  // scene-lifetime device allocations
+    dt::Scratch scratch;
+    bool counters = false;
+    uint64_t queue_cap = 0;  // 0: automatic
+    dtrt_render_stats last{};
+    int num_shapes = 0;
+    std::vector<float> shape_edge_len;  // per shape total edge length (for re-weighting)
+    std::vector<int> shape_skip;        // null-BSDF shapes without emitter
+};
+
+namespace dt {
+template <int N>
+int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream);
+bool ensure_buffer(void **ptr, size_t *have, size_t need);
+}  // namespace dt

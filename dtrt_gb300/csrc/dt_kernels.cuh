@@ -1,0 +1,750 @@
+// dtrt_gb300 — forward-mode render kernels (templated on the derivative width N).
+//
+// The reference evaluates VolPathTracerAD::LiAD (volpathAD.cpp:145-620) recursively and
+// estimates its boundary terms inline, each edge sample tracing two full Li sub-paths.
+// Every contribution is additive into the pixel with a weight known when it is spawned,
+// so the recursion flattens into task queues:
+//
+//   k_camera   one thread per camera path sample: the LiAD chain as a loop carrying a
+//              dual prefix throughput; emits EdgeRec (surface / volume edge term) and
+//              LinsRec (Lins interface term) records instead of recursing
+//   k_edge     one thread per (edge record, edge sample): FP64 silhouette test and
+//              edge-point solve, the visibility gate, then two LiTask sub-paths
+//   k_lins     one thread per Lins record: the Lins estimate with its Li sub-paths
+//   k_primary  one thread per primary-edge sample (integratorAD.cpp:100-165)
+//   k_li       one thread per LiTask: the non-AD path Li (volpathAD.cpp:50-142), whose
+//              result L adds s_j * w_c * L_c to derivative slot j of its pixel
+//   k_finalize FP64 accumulators -> float image with the reference's write rules
+//
+// All pushes are warp-aggregated (ballot + popc, one atomic per warp); a push past a
+// queue's capacity sets an error flag and is dropped, never written out of bounds.
+#pragma once
+#include "dt_device.cuh"
+
+namespace dt {
+
+struct RenderParams {
+    uint64_t seed;
+    int spp, max_bounces, sppse, mode, jitter;
+    float ddist, inv_spp;
+    int npix, out_w, out_h, crop_x, crop_y;
+    long long path_begin, path_count;
+    double prim_weight;  // primary-edge PDF sum / sample count
+    long long prim_begin, prim_count;
+};
+
+template <int N>
+struct EdgeRec {
+    float x0[3], x0d[N][3];
+    float w[3];      // prefix throughput value / spp
+    float wi[3];     // surface: local incident direction; volume: world -ray.dir
+    float fs[3], ft[3], fn[3], ng[3];
+    int kind, shape, med, phase, depth, pixel;
+    uint64_t key;
+};
+
+template <int N>
+struct LinsRec {
+    float p[3], ng[3], n[3], rd[3], fs[3], ft[3], fn[3], wi[3];
+    float w[3];      // prefix throughput * sigma_s / (spp * nsamples)
+    float s[N];      // hit-distance derivative slots
+    int shape, med, phase, depth, pixel, ns;
+    uint64_t key;
+};
+
+template <int N>
+struct LiTask {
+    float o[3], d[3], w[3], s[N];
+    int med, depth, pixel, flags;  // flags: bit0 include emission, bit1 primary-edge image
+    uint64_t key;
+};
+
+struct Queue {
+    void *data;
+    unsigned long long *count;
+    unsigned long long cap;
+};
+
+// Counter slots (dtrt_render_stats order)
+enum { CT_RAYS = 0, CT_NODES, CT_TRIS, CT_LOOKUPS, CT_EDGE_SAMPLES, CT_LI, CT_PRIMARY, CT_NUM };
+
+DT_D void flush_counters(unsigned long long *ctr, const Ctr &c, uint32_t extra_slot = 0xffffffffu, uint32_t extra = 0) {
+    if (!ctr) return;
+    unsigned long long v[4] = {c.rays, c.nodes, c.tris, c.lookups};
+    const unsigned mask = __activemask();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        unsigned long long x = v[k];
+        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(mask, x, off);
+        v[k] = x;
+    }
+    if ((threadIdx.x & 31) == (__ffs(mask) - 1)) {
+        for (int k = 0; k < 4; ++k)
+            if (v[k]) atomicAdd(ctr + k, v[k]);
+    }
+    if (extra_slot != 0xffffffffu && extra) atomicAdd(ctr + extra_slot, (unsigned long long)extra);
+}
+
+// warp-aggregated slot reservation: returns the slot index or -1 on overflow
+DT_D long long queue_reserve(const DevScene &sc, const Queue &q) {
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    const unsigned rank = __popc(mask & ((1u << lane) - 1u));
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(q.count, (unsigned long long)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    const unsigned long long slot = base + rank;
+    if (slot >= q.cap) {
+        set_error(sc, ERR_QUEUE);
+        return -1;
+    }
+    return (long long)slot;
+}
+
+// camera.cpp:52-60 / 75-83 / 40-50
+DT_D void camera_ray(const DevCamera &cam, double x, double y, float3 &o, float3 &d) {
+    const double sx = x / cam.width, sy = y / cam.height, aspect = (double)cam.width / cam.height;
+    const float3 ndc = mk((float)((sx - 0.5) * 2.0), (float)((sy - 0.5) * (-2.0) / aspect), 1.f);
+    const float *m = cam.ndc2cam;
+    float3 dc = normalize(mk(m[0] * ndc.x + m[1] * ndc.y + m[2] * ndc.z, m[3] * ndc.x + m[4] * ndc.y + m[5] * ndc.z,
+                             m[6] * ndc.x + m[7] * ndc.y + m[8] * ndc.z));
+    const float *c = cam.c2w;
+    o = mk(c[3], c[7], c[11]);
+    d = mk(c[0] * dc.x + c[1] * dc.y + c[2] * dc.z, c[4] * dc.x + c[5] * dc.y + c[6] * dc.z,
+           c[8] * dc.x + c[9] * dc.y + c[10] * dc.z);
+}
+template <int N>
+DT_D RayAD<N> camera_ray_ad(const DevCamera &cam, double x, double y) {
+    const double sx = x / cam.width, sy = y / cam.height, aspect = (double)cam.width / cam.height;
+    const float3 ndc = mk((float)((sx - 0.5) * 2.0), (float)((sy - 0.5) * (-2.0) / aspect), 1.f);
+    const float *m = cam.ndc2cam;
+    const float3 dc = normalize(mk(m[0] * ndc.x + m[1] * ndc.y + m[2] * ndc.z,
+                                   m[3] * ndc.x + m[4] * ndc.y + m[5] * ndc.z,
+                                   m[6] * ndc.x + m[7] * ndc.y + m[8] * ndc.z));
+    RayAD<N> r;
+    r.o = DV<N>(f3(cam.cpos));
+    DV<N> s(f3(cam.cframe[0])), t(f3(cam.cframe[1])), n(f3(cam.cframe[2]));
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        r.o.set_grad(j, f3(cam.d_cpos[j]));
+        s.set_grad(j, f3(cam.d_cframe[j][0]));
+        t.set_grad(j, f3(cam.d_cframe[j][1]));
+        n.set_grad(j, f3(cam.d_cframe[j][2]));
+    }
+    r.d = s * dc.x + t * dc.y + n * dc.z;
+    return r;
+}
+
+// ====================================================================== camera AD paths
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_camera(DevScene sc, RenderParams rp, Queue qe, Queue ql, double *acc1,
+                                                   unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < rp.path_count;
+    const long long g = rp.path_begin + (active ? gi : 0);
+    const int pixel = (int)(g / rp.spp);
+    const int sample = (int)(g % rp.spp);
+    Ctr c;
+    DV<N> acc;
+    if (active) {
+        const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
+        const uint64_t key = (uint64_t)g;
+        Rng rng;
+        rng.init(rp.seed, key);
+        double jx = 0.5, jy = 0.5;
+        if (rp.jitter) {
+            jx = rng.next1d();
+            jy = rng.next1d();
+        }
+        RayAD<N> ray = camera_ray_ad<N>(sc.cam, ix + jx, iy + jy);
+        ItsAD<N> its;
+        int med = sc.cam.med_id;
+        int depth = rp.max_bounces;
+        int mode = rp.mode;
+        DV<N> P(mk(1.f, 1.f, 1.f));
+        bool alive = ray_intersect_ad<N>(sc, stack, ray, false, its, c);
+        for (int level = 0; alive && mode != 0; ++level) {
+            alive = false;
+            const float r1a = rng.next1(), r1b = rng.next1();
+            float r2[4];
+            r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
+            const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
+            DV<N> thr(mk(1.f, 1.f, 1.f));
+            const float3 dir_in = ray.d.val();
+            if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c)) {
+                // ------------------------------------------------ volumetric vertex, volpathAD.cpp:164-305
+                if (depth == 0 || thr.is_zero()) break;
+                const DevPhase &ph = sc.phases[sc.media[med].phase_id];
+                const DV<N> Q = cmul(P, thr);
+                DV<N> wo;
+                float pdf_nee;
+                if (mode & MODE_VOLUME_MAIN) {
+                    DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
+                    if (!v.is_zero()) {
+                        Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+                        if (pv.v > kEps) acc += cmul(Q, v) * (pv * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
+                    }
+                }
+                // edge record before the continuation overwrites the vertex state
+                if (rp.sppse > 0 && (mode & MODE_VOLUME_BOUNDARY2) && sc.has_edges &&
+                    (sc.moving_geometry || !ray.o.der_zero(0.f))) {
+                    const long long slot = queue_reserve(sc, qe);
+                    if (slot >= 0) {
+                        EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
+                        const float3 x = ray.o.val(), w = cmul(P.val(), thr.val()) * rp.inv_spp, wi = -dir_in;
+                        r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
+#pragma unroll
+                        for (int j = 0; j < N; ++j) {
+                            const float3 gj = ray.o.grad(j);
+                            r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
+                        }
+                        r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+                        r.wi[0] = wi.x; r.wi[1] = wi.y; r.wi[2] = wi.z;
+                        r.kind = 1; r.shape = -1; r.med = med; r.phase = sc.media[med].phase_id;
+                        r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 1u, (uint32_t)level);
+                    }
+                }
+                const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
+                if (pvs.v > kEps) {
+                    const DV<N> thr1 = thr * pvs;
+                    ray.d = wo;
+                    ItsAD<N> its1;
+                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
+                                                       nullptr, c);
+                    if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+                        acc += cmul(cmul(P, thr1), att) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+                    its = its1;
+                    P = cmul(P, thr1);
+                    depth -= 1;
+                    mode &= ~MODE_EMISSION;
+                    alive = true;
+                }
+                continue;
+            }
+            // ---------------------------------------------------- interface vertex, volpathAD.cpp:306-617
+            if (!its.valid() || thr.is_zero()) break;
+            const DevShape &sh = sc.shapes[its.shape];
+            if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) break;
+            const DV<N> Q = cmul(P, thr);
+            if (sh.light_id >= 0 && (mode & MODE_EMISSION)) acc += cmul(Q, le_ad<N>(sc, its, -ray.d));
+            if (depth == 0) break;
+            const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
+            const bool is_null = b.type == BSDF_NULL;
+            const FrameAD<N> fr = its.frame();
+            const Its its0 = its.plain();
+            // Lins boundary term, volpathAD.cpp:321-467
+            if (med >= 0 && !its.t.der_zero(kDerZeroEps) && (mode & MODE_VOLUME_BOUNDARY1)) {
+                const long long slot = queue_reserve(sc, ql);
+                if (slot >= 0) {
+                    LinsRec<N> &r = reinterpret_cast<LinsRec<N> *>(ql.data)[slot];
+                    float3 n = its0.ng;
+                    if (dot(n, dir_in) < 0.f) n = -n;
+                    const int ns = min(max((int)(rp.ddist * its.t.der_max()), 1), 100);
+                    const float3 sig = sig_s(sc.media[med], its0.p - n * kShadowEps, c);
+                    const float3 w = cmul(cmul(P.val(), thr.val()), sig) * (rp.inv_spp / (float)ns);
+                    const float3 *src[8] = {&its0.p, &its0.ng, &n, &dir_in, &its0.fr.s, &its0.fr.t, &its0.fr.n, &its0.wi};
+                    float *dst[8] = {r.p, r.ng, r.n, r.rd, r.fs, r.ft, r.fn, r.wi};
+                    for (int k = 0; k < 8; ++k) { dst[k][0] = src[k]->x; dst[k][1] = src[k]->y; dst[k][2] = src[k]->z; }
+                    r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+#pragma unroll
+                    for (int j = 0; j < N; ++j) r.s[j] = its.t.d[j];
+                    r.shape = its.shape; r.med = med; r.phase = sc.media[med].phase_id; r.depth = depth;
+                    r.pixel = pixel; r.ns = ns; r.key = child_key(key, 2u, (uint32_t)level);
+                }
+            }
+            // interface edge record, volpathAD.cpp:513-616
+            if (!is_null && rp.sppse > 0 && (mode & MODE_SURFACE_BOUNDARY) && sc.has_edges &&
+                (sc.moving_geometry || !its.p.der_zero(0.f))) {
+                const long long slot = queue_reserve(sc, qe);
+                if (slot >= 0) {
+                    EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
+                    const float3 x = its0.p, w = cmul(P.val(), thr.val()) * rp.inv_spp;
+                    r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
+#pragma unroll
+                    for (int j = 0; j < N; ++j) {
+                        const float3 gj = its.p.grad(j);
+                        r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
+                    }
+                    r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+                    r.wi[0] = its0.wi.x; r.wi[1] = its0.wi.y; r.wi[2] = its0.wi.z;
+                    r.fs[0] = its0.fr.s.x; r.fs[1] = its0.fr.s.y; r.fs[2] = its0.fr.s.z;
+                    r.ft[0] = its0.fr.t.x; r.ft[1] = its0.fr.t.y; r.ft[2] = its0.fr.t.z;
+                    r.fn[0] = its0.fr.n.x; r.fn[1] = its0.fr.n.y; r.fn[2] = its0.fr.n.z;
+                    r.ng[0] = its0.ng.x; r.ng[1] = its0.ng.y; r.ng[2] = its0.ng.z;
+                    r.kind = 0; r.shape = its.shape; r.med = med; r.phase = -1;
+                    r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 3u, (uint32_t)level);
+                }
+            }
+            // area sampling, volpathAD.cpp:469-511
+            DV<N> wo;
+            float pdf_nee;
+            if (!is_null && (mode & MODE_SURFACE_MAIN)) {
+                DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+                if (!v.is_zero()) {
+                    const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
+                    const float bp = bsdf_pdf(b, its0.wi, wo.val());
+                    acc += cmul(cmul(Q, v), bv) * mis_weight(pdf_nee, bp);
+                }
+            }
+            float bpdf, beta;
+            const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
+            if (!bw.is_zero()) {
+                wo = fr.to_world(wo);
+                if (!is_null) wo = zero_grad(wo);  // asserted zero in the reference (volpathAD.cpp:489)
+                ray.o = its.p;
+                ray.d = wo;
+                const int med1 = is_transition(sh) ? target_medium(sc, its.shape, its.ng, wo.val()) : med;
+                DV<N> thr1 = thr;
+                ItsAD<N> its1;
+                if (is_null) {
+                    ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
+                } else {
+                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee,
+                                                       nullptr, nullptr, c);
+                    thr1 = cmul(thr1, bw);
+                    if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
+                        acc += cmul(cmul(P, thr1), att) * mis_weight(bpdf, pdf_nee);
+                    mode &= ~MODE_EMISSION;
+                }
+                its = its1;
+                P = cmul(P, thr1);
+                med = med1;
+                depth -= 1;
+                alive = true;
+            }
+        }
+        acc = acc * rp.inv_spp;
+    }
+    // accumulate: a warp whose 32 lanes share one pixel reduces with shuffles first
+    const unsigned full = 0xffffffffu;
+    const int p0 = __shfl_sync(full, pixel, 0);
+    const bool uniform = __all_sync(full, active && pixel == p0);
+    float vals[3 * (N + 1)];
+    vals[0] = acc.x.v; vals[1] = acc.y.v; vals[2] = acc.z.v;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        vals[3 * (j + 1)] = acc.x.d[j];
+        vals[3 * (j + 1) + 1] = acc.y.d[j];
+        vals[3 * (j + 1) + 2] = acc.z.d[j];
+    }
+    if (uniform) {
+#pragma unroll
+        for (int k = 0; k < 3 * (N + 1); ++k) {
+            float x = vals[k];
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(full, x, off);
+            vals[k] = x;
+        }
+    }
+    if (active && (!uniform || (threadIdx.x & 31) == 0)) {
+#pragma unroll
+        for (int k = 0; k < 3 * (N + 1); ++k) {
+            if (vals[k] != 0.f) atomicAdd(acc1 + ((size_t)(k / 3) * rp.npix + pixel) * 3 + (k % 3), (double)vals[k]);
+        }
+    }
+    if (ctr) flush_counters(ctr, c);
+}
+
+// ====================================================================== FP64 edge geometry
+struct EdgeGeom {
+    double w1[3], nrm[3];
+    double dist, pdf;
+};
+
+// pmf.h:103-167 sampleReuse on a normalised CDF with a leading 0 (n+1 entries)
+DT_D int sample_reuse(const double *cdf, int n, double &u, double &pdf) {
+    int lo = 0, hi = n + 1;  // lower_bound
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (cdf[mid] < u) lo = mid + 1;
+        else hi = mid;
+    }
+    int idx = min(n - 1, max(0, lo - 1));
+    while (cdf[idx + 1] - cdf[idx] == 0.0 && idx < n - 1) ++idx;
+    pdf = cdf[idx + 1] - cdf[idx];
+    u = (u - cdf[idx]) / pdf;
+    return idx;
+}
+
+// shape.cpp:302-335
+DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) {
+    if (e.f0 < 0 || e.f1 < 0) return 2;
+    const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
+    bool ff[2] = {false, false};
+    for (int k = 0; k < 2; ++k) {
+        const int4 tri = __ldg(sc.tris + (k == 0 ? e.f0 : e.f1));
+        const int ids[3] = {tri.x, tri.y, tri.z};
+        for (int i = 0; i < 3; ++i) {
+            if (ids[i] != e.v0 && ids[i] != e.v1) {
+                const double3_ v = tod(f3(__ldg(sc.verts + ids[i])));
+                const double3_ n = k == 0 ? normalized(crossd(v0 - v, v1 - v)) : normalized(crossd(v1 - v, v0 - v));
+                ff[k] = dotd(n, p - v) > 0.0;
+                break;
+            }
+        }
+    }
+    if (ff[0] != ff[1]) return 2;
+    return sc.shapes[e.shape].has_normals ? 0 : 1;
+}
+
+// volpathAD.cpp:231-280 / 540-589 (ALTERNATIVE_EDGE_SAMPLING): the angularly interpolated
+// direction to the edge point, its derivative slots and the angular pdf, all in FP64.
+template <int N>
+DT_D bool edge_direction(const DevScene &sc, const DevEdge &e, const double3_ &x0, const double (*x0d)[3], double t,
+                         double &pdf, double3_ &w1, double (*w1d)[3], double &dist, double3_ &nrm) {
+    const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
+    const double3_ e0 = v0 - x0, e1 = v1 - x0;
+    nrm = normalized(crossd(e0, e1));
+    const double l0 = lengthd(e0), l1 = lengthd(e1);
+    const double c = fmin(1.0, fmax(-1.0, dotd(e0, e1) / (l0 * l1)));
+    const double theta = acos(c), st = sin(theta);
+    if (theta < kEpsD || theta > kPiD - kEpsD) return false;
+    double w0 = sin(theta * (1.0 - t)) / st / l0, wb = sin(theta * t) / st / l1;
+    const double tmp = w0 + wb;
+    w0 /= tmp;
+    wb /= tmp;
+    if (w0 < -kEpsD || wb < -kEpsD || fabs(w0 + wb - 1.0) > kEpsD) return false;
+    const double3_ w = e0 * w0 + e1 * wb;
+    dist = lengthd(w);
+    w1 = w * (1.0 / dist);
+    double mx = 0.0;
+    for (int j = 0; j < N; ++j) {
+        double dv0[3] = {0, 0, 0}, dv1[3] = {0, 0, 0};
+        if (sc.vert_der) {
+            const float *g0 = sc.vert_der + (size_t)e.v0 * sc.nder * 3 + 3 * j;
+            const float *g1 = sc.vert_der + (size_t)e.v1 * sc.nder * 3 + 3 * j;
+            for (int k = 0; k < 3; ++k) { dv0[k] = g0[k]; dv1[k] = g1[k]; }
+        }
+        double dw[3];
+        for (int k = 0; k < 3; ++k) dw[k] = (dv0[k] - x0d[j][k]) * w0 + (dv1[k] - x0d[j][k]) * wb;
+        const double proj = w1.x * dw[0] + w1.y * dw[1] + w1.z * dw[2];
+        w1d[j][0] = (dw[0] - w1.x * proj) / dist;
+        w1d[j][1] = (dw[1] - w1.y * proj) / dist;
+        w1d[j][2] = (dw[2] - w1.z * proj) / dist;
+        mx = fmax(mx, fabs(w1d[j][0] * w1.x + w1d[j][1] * w1.y + w1d[j][2] * w1.z));
+    }
+    pdf /= theta;
+    return !(mx > kEpsD);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Queue qe, long long rec_begin,
+                                                 long long rec_count, Queue qli, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    uint32_t nsamples = 0;
+    if (gi < rec_count * rp.sppse) {
+        const long long ri = rec_begin + gi / rp.sppse;
+        const int i = (int)(gi % rp.sppse);
+        const EdgeRec<N> &r = reinterpret_cast<const EdgeRec<N> *>(qe.data)[ri];
+        Rng rng;
+        rng.init(rp.seed, child_key(r.key, 7u, (uint32_t)i));
+        nsamples = 1;
+        double u = ((double)i + rng.next1d()) / rp.sppse;
+        double pdf_shape, pdf_edge;
+        const int sid = sample_reuse(sc.shape_edge_cdf, sc.num_shapes, u, pdf_shape);
+        const DevShape &shp = sc.shapes[sid];
+        const bool has = shp.num_edges > 0;
+        const int k = has ? sample_reuse(sc.edge_cdf + shp.edge_cdf_off, shp.num_edges, u, pdf_edge) : 0;
+        double pdf = has ? pdf_shape * pdf_edge : 0.0;
+        const DevEdge e = sc.edges[shp.edge_off + (has ? k : 0)];
+        const double3_ x0 = mkd(r.x0[0], r.x0[1], r.x0[2]);
+        bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL && is_silhouette(sc, e, x0) > 0;
+        double x0d[N][3];
+#pragma unroll
+        for (int j = 0; j < N; ++j)
+            for (int q = 0; q < 3; ++q) x0d[j][q] = r.x0d[j][q];
+        double3_ w1, nrm;
+        double w1d[N][3], dist;
+        if (ok) ok = edge_direction<N>(sc, e, x0, x0d, u, pdf, w1, w1d, dist, nrm);
+        if (ok) {
+            bool dz = true;
+            for (int j = 0; j < N; ++j)
+                for (int q = 0; q < 3; ++q) dz = dz && fabs(w1d[j][q]) <= kEpsD;
+            ok = !dz;
+        }
+        float3 val = mk(0.f, 0.f, 0.f);
+        int med1 = r.med;
+        const float3 w1f = tof(w1);
+        if (ok) {
+            if (r.kind == 0) {
+                Frame fr;
+                fr.s = f3(r.fs); fr.t = f3(r.ft); fr.n = f3(r.fn);
+                const DevShape &vs = sc.shapes[r.shape];
+                val = cmul(f3(r.w), bsdf_eval(sc.bsdfs[vs.bsdf_id], f3(r.wi), fr.to_local(w1f)));
+                if (is_transition(vs)) med1 = dot(w1f, f3(r.ng)) > 0.f ? vs.med_ext : vs.med_int;
+            } else {
+                val = f3(r.w) * phase_eval(sc.phases[r.phase], f3(r.wi), w1f);
+            }
+            ok = !is_zero3(val);
+        }
+        if (ok) {
+            const float tr = eval_transmittance(sc, stack, tof(x0), w1f, r.kind == 0, med1, (float)dist, rng, r.depth, c);
+            ok = tr > kEps;
+        }
+        if (ok) {
+            float s[N];
+            const double k2 = 1.0 / (pdf * rp.sppse);
+#pragma unroll
+            for (int j = 0; j < N; ++j) s[j] = (float)((nrm.x * w1d[j][0] + nrm.y * w1d[j][1] + nrm.z * w1d[j][2]) * k2);
+            for (int sgn = 0; sgn < 2; ++sgn) {
+                const double a = sgn == 0 ? -(double)kAngleEps : (double)kAngleEps;
+                const double3_ w2 = normalized(w1 + nrm * a);
+                const long long slot = queue_reserve(sc, qli);
+                if (slot < 0) continue;
+                LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot];
+                t.o[0] = (float)x0.x; t.o[1] = (float)x0.y; t.o[2] = (float)x0.z;
+                t.d[0] = (float)w2.x; t.d[1] = (float)w2.y; t.d[2] = (float)w2.z;
+                const float sg = sgn == 0 ? 1.f : -1.f;
+                t.w[0] = val.x * sg; t.w[1] = val.y * sg; t.w[2] = val.z * sg;
+#pragma unroll
+                for (int j = 0; j < N; ++j) t.s[j] = s[j];
+                t.med = med1; t.depth = r.depth; t.pixel = r.pixel; t.flags = 1;
+                t.key = child_key(r.key, 8u + (uint32_t)sgn, (uint32_t)i);
+            }
+        }
+    }
+    if (ctr) flush_counters(ctr, c, CT_EDGE_SAMPLES, nsamples);
+}
+
+// ====================================================================== Li sub-paths
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_li(DevScene sc, RenderParams rp, Queue qli, long long begin, long long count,
+                                               double *acc1, double *acc2, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    uint32_t n = 0;
+    if (gi < count) {
+        const LiTask<N> &t = reinterpret_cast<const LiTask<N> *>(qli.data)[begin + gi];
+        Rng rng;
+        rng.init(rp.seed, t.key);
+        n = 1;
+        const float3 L = li_path(sc, stack, rng, f3(t.o), f3(t.d), t.depth, t.med, (t.flags & 1) != 0, c);
+        if (!is_zero3(L, 0.f)) {
+            const float3 wl = cmul(f3(t.w), L);
+            const bool prim = (t.flags & 2) != 0;
+            double *acc = prim ? acc2 : acc1 + (size_t)rp.npix * 3;  // slot j of the derivative images
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                if (t.s[j] == 0.f) continue;
+                double *a = acc + ((size_t)j * rp.npix + t.pixel) * 3;
+                atomicAdd(a, (double)(wl.x * t.s[j]));
+                atomicAdd(a + 1, (double)(wl.y * t.s[j]));
+                atomicAdd(a + 2, (double)(wl.z * t.s[j]));
+            }
+        }
+    }
+    if (ctr) flush_counters(ctr, c, CT_LI, n);
+}
+
+// ====================================================================== Lins records
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_lins(DevScene sc, RenderParams rp, Queue ql, long long count, double *acc1,
+                                                 unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    if (gi < count) {
+        const LinsRec<N> &r = reinterpret_cast<const LinsRec<N> *>(ql.data)[gi];
+        Rng rng;
+        rng.init(rp.seed, r.key);
+        Its its0;
+        its0.shape = r.shape; its0.p = f3(r.p); its0.ng = f3(r.ng); its0.wi = f3(r.wi);
+        its0.fr.s = f3(r.fs); its0.fr.t = f3(r.ft); its0.fr.n = f3(r.fn);
+        const float3 n = f3(r.n), rd = f3(r.rd);
+        const DevPhase &ph = sc.phases[r.phase];
+        const DevShape &sh = sc.shapes[r.shape];
+        const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
+        const int max_depth = r.depth, med = r.med;
+        float3 lins = mk(0.f, 0.f, 0.f);
+        for (int smp = 0; smp < r.ns; ++smp) {  // volpathAD.cpp:337-441
+            float3 wo, att;
+            float pdf_nee, pv;
+            Its its1;
+            float r4[4];
+            r4[0] = rng.next1(); r4[1] = rng.next1(); r4[2] = rng.next1(); r4[3] = rng.next1();
+            if (b.type == BSDF_NULL) {
+                att = nee_surface(sc, stack, its0, r4, rng, med, max_depth - 1, wo, pdf_nee, true, c);
+                if (!is_zero3(att)) {
+                    wo = its0.to_world(wo);
+                    pv = phase_eval(ph, -rd, wo);
+                    if (pv > kEps) lins += att * (pv * mis_weight(pdf_nee, pv));
+                }
+                const float u = rng.next1(), v = rng.next1();
+                if ((pv = phase_sample(ph, -rd, u, v, wo)) > kEps) {
+                    int md1 = max_depth - 1;
+                    if (dot(wo, n) > kEps) {
+                        if (sh.light_id >= 0) lins += le(sc, its0, -wo) * pv;
+                        --md1;
+                    }
+                    if (md1 > 0) {
+                        const int med1 = is_transition(sh) ? target_medium(sc, r.shape, its0.ng, wo) : med;
+                        att = look_for_emitter(sc, stack, its0.p, wo, true, rng, med1, md1, its1, pdf_nee, c);
+                        if (!is_zero3(att)) lins += att * (pv * mis_weight(phase_eval(ph, -rd, wo), pdf_nee));
+                        lins += li_path(sc, stack, rng, its0.p, wo, md1, med1, false, c) * pv;
+                    }
+                }
+                continue;
+            }
+            att = nee_surface(sc, stack, its0, r4, rng, med, max_depth - 1, wo, pdf_nee, false, c);
+            if (!is_zero3(att)) {
+                wo = its0.to_world(wo);
+                if (dot(wo, n) < -kEps) {
+                    pv = phase_eval(ph, -rd, wo);
+                    if (pv > kEps) lins += att * (pv * mis_weight(pdf_nee, pv));
+                }
+            }
+            const float u = rng.next1(), v = rng.next1();
+            if ((pv = phase_sample(ph, -rd, u, v, wo)) > kEps) {
+                const float wdn = dot(wo, n);
+                if (wdn < -kEps) {
+                    att = look_for_emitter(sc, stack, its0.p, wo, true, rng, med, max_depth - 1, its1, pdf_nee, c);
+                    if (!is_zero3(att)) lins += att * (pv * mis_weight(phase_eval(ph, -rd, wo), pdf_nee));
+                    lins += li_path(sc, stack, rng, its0.p, wo, max_depth - 1, med, false, c) * pv;
+                } else if (wdn > kEps) {
+                    if (sh.light_id >= 0) lins += le(sc, its0, -wo) * pv;
+                    if (max_depth > 1) {
+                        Its its2 = its0;
+                        its2.wi = its2.to_local(-wo);
+                        float r4b[4];
+                        r4b[0] = rng.next1(); r4b[1] = rng.next1(); r4b[2] = rng.next1(); r4b[3] = rng.next1();
+                        att = nee_surface(sc, stack, its2, r4b, rng, med, max_depth - 2, wo, pdf_nee, false, c);
+                        if (!is_zero3(att))
+                            lins += cmul(bsdf_eval(b, its2.wi, wo), att) *
+                                    (pv * mis_weight(pdf_nee, bsdf_pdf(b, its2.wi, wo)));
+                        const float ra = rng.next1(), rb = rng.next1(), rc = rng.next1();
+                        float bp, eta;
+                        const float3 bv = bsdf_sample(b, its2.wi, ra, rb, rc, wo, bp, eta);
+                        if (!is_zero3(bv)) {
+                            const float3 t1 = bv * pv;
+                            wo = its2.to_world(wo);
+                            const int med1 = is_transition(sh) ? target_medium(sc, r.shape, its2.ng, wo) : med;
+                            Its its3;
+                            att = look_for_emitter(sc, stack, its2.p, wo, true, rng, med1, max_depth - 2, its3, pdf_nee, c);
+                            if (!is_zero3(att, 1e-12f)) lins += cmul(t1, att) * mis_weight(bp, pdf_nee);
+                            lins += cmul(t1, li_path(sc, stack, rng, its2.p, wo, max_depth - 2, med1, false, c));
+                        }
+                    }
+                }
+            }
+        }
+        const float3 wl = cmul(f3(r.w), lins);
+        if (!is_zero3(wl, 0.f)) {
+            double *acc = acc1 + (size_t)rp.npix * 3;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                double *a = acc + ((size_t)j * rp.npix + r.pixel) * 3;
+                atomicAdd(a, (double)(wl.x * r.s[j]));
+                atomicAdd(a + 1, (double)(wl.y * r.s[j]));
+                atomicAdd(a + 2, (double)(wl.z * r.s[j]));
+            }
+        }
+    }
+    if (ctr) flush_counters(ctr, c);
+}
+
+// ====================================================================== primary edges
+// compute_intersection_in_tri, utils.cpp:256-266
+DT_D double intersection_in_tri(const double *b0, const double *c0, const double *b1, const double *c1, double t0) {
+    auto nrm = [](const double *a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); };
+    const double cb = nrm(b0) / nrm(b1), cc = nrm(c0) / nrm(c1);
+    const double bx = (1.0 - t0) * cb, by = t0 * cc;
+    return by / (bx + by);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp, Queue qli, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    uint32_t n = 0;
+    if (gi < rp.prim_count) {
+        const long long k = rp.prim_begin + gi;
+        Rng rng;
+        rng.init(rp.seed, child_key(0x5052494DULL, (uint32_t)(k >> 32), (uint32_t)k));
+        n = 1;
+        // edge_manager.cpp:112-134
+        double u = rng.next1d(), pdf;
+        const int idx = sample_reuse(sc.pedge_cdf, sc.num_pedges, u, pdf);
+        const DevPrimaryEdge &e = sc.pedges[idx];
+        const DevCamera &cam = sc.cam;
+        double px_ = e.v0s[0] + (e.v1s[0] - e.v0s[0]) * u, py_ = e.v0s[1] + (e.v1s[1] - e.v0s[1]) * u;
+        float pdx[N], pdy[N];
+        bool moving = false;
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            pdx[j] = (float)(e.d0[j][0] + (e.d1[j][0] - e.d0[j][0]) * u);
+            pdy[j] = (float)(e.d0[j][1] + (e.d1[j][1] - e.d0[j][1]) * u);
+            moving = moving || fabsf(pdx[j]) > kEps || fabsf(pdy[j]) > kEps;
+        }
+        const double fov = cam.fov, aspect = (double)cam.width / cam.height;
+        const double tmp[3] = {(px_ / cam.width - 0.5) * 2.0 / fov, (py_ / cam.height - 0.5) * (-2.0) / (aspect * fov), 1.0};
+        const int ipx = (int)floor(px_), ipy = (int)floor(py_);
+        double nx = e.v1s[1] - e.v0s[1], ny = e.v0s[0] - e.v1s[0];
+        const double nl = sqrt(nx * nx + ny * ny);
+        nx /= nl;
+        ny /= nl;
+        const double fx = px_ - ipx, fy = py_ - ipy;
+        double a[3], bb[3];
+        for (int q = 0; q < 3; ++q) { a[q] = tmp[q] - e.v0p[q]; bb[q] = e.v1p[q] - e.v0p[q]; }
+        const double t0 = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) / sqrt(bb[0] * bb[0] + bb[1] * bb[1] + bb[2] * bb[2]);
+        const double t1 = intersection_in_tri(e.v0p, e.v1p, e.v0c, e.v1c, t0);
+        double pc[3];
+        for (int q = 0; q < 3; ++q) pc[q] = e.v0c[q] + t1 * (e.v1c[q] - e.v0c[q]);
+        const float maxd = (float)sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+        const int lx = ipx - rp.crop_x, ly = ipy - rp.crop_y;
+        if (moving && lx >= 0 && ly >= 0 && lx < rp.out_w && ly < rp.out_h) {
+            float3 o, d;
+            camera_ray(cam, ipx + fx, ipy + fy, o, d);
+            const float tr = eval_transmittance(sc, stack, o, d, false, cam.med_id, maxd, rng, rp.max_bounces - 1, c);
+            if (tr > kEps) {
+                for (int sgn = 0; sgn < 2; ++sgn) {
+                    const double delta = sgn == 0 ? -1e-4 : 1e-4;
+                    float3 o2, d2;
+                    camera_ray(cam, ipx + fx + nx * delta, ipy + fy + ny * delta, o2, d2);
+                    const long long slot = queue_reserve(sc, qli);
+                    if (slot < 0) continue;
+                    LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot];
+                    t.o[0] = o2.x; t.o[1] = o2.y; t.o[2] = o2.z;
+                    t.d[0] = d2.x; t.d[1] = d2.y; t.d[2] = d2.z;
+                    const float w = (float)(sgn == 0 ? rp.prim_weight : -rp.prim_weight);
+                    t.w[0] = w; t.w[1] = w; t.w[2] = w;
+#pragma unroll
+                    for (int j = 0; j < N; ++j) t.s[j] = (float)(nx * pdx[j] + ny * pdy[j]);
+                    t.med = cam.med_id; t.depth = rp.max_bounces; t.pixel = lx + rp.out_w * ly; t.flags = 1 | 2;
+                    t.key = child_key(0x50524D31ULL + (uint64_t)k, 9u + (uint32_t)sgn, 0u);
+                }
+            }
+        }
+    }
+    if (ctr) flush_counters(ctr, c, CT_PRIMARY, n);
+}
+
+// ====================================================================== finalize
+// integratorAD.cpp:59-87 and 154-162: a pixel is written only if its value is
+// non-negative, a derivative only if finite; primary-edge sums are then added.
+template <int N>
+__global__ void k_finalize(RenderParams rp, const double *acc1, const double *acc2, float *out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= rp.npix) return;
+    const double *a = acc1 + (size_t)p * 3;
+    const bool nonneg = a[0] >= 0.0 && a[1] >= 0.0 && a[2] >= 0.0;
+    for (int c = 0; c < 3; ++c) out[(size_t)p * 3 + c] = nonneg ? (float)a[c] : 0.f;
+    for (int j = 0; j < N; ++j) {
+        const double *d = acc1 + ((size_t)(j + 1) * rp.npix + p) * 3;
+        const bool fin = isfinite(d[0]) && isfinite(d[1]) && isfinite(d[2]);
+        const double *e = acc2 + ((size_t)j * rp.npix + p) * 3;
+        for (int c = 0; c < 3; ++c)
+            out[((size_t)(j + 1) * rp.npix + p) * 3 + c] = (fin ? (float)d[c] : 0.f) + (float)e[c];
+    }
+}
+
+}  // namespace dt

@@ -1,0 +1,216 @@
+// dtrt_gb300 — render orchestration for one derivative width (instantiated per N).
+//
+// IntegratorAD::render (integratorAD.cpp:19-166) as batches of camera paths:
+//   for each batch:   k_camera -> [k_edge -> k_li]* (chunked) -> k_lins
+//   primary edges:    [k_primary -> k_li]* (chunked)
+//   k_finalize
+// Queue capacities bound device memory; the worst case per camera path (one edge or
+// Lins record per bounce, two Li tasks per edge sample) sizes the batches so that a
+// push can only overflow when a caller forces a capacity below one path's worst case.
+#pragma once
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "dt_host.h"
+
+namespace dt {
+
+#define DT_CK(call)                                                                  \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_));      \
+            return DTRT_ERR_CUDA;                                                    \
+        }                                                                            \
+    } while (0)
+
+template <int N>
+int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t st) {
+    using clk = std::chrono::steady_clock;
+    const auto t_start = clk::now();
+    DevScene sc = s->dev;
+    Scratch &sb = s->scratch;
+    const DevCamera &cam = sc.cam;
+    const bool cropped = cam.crop_w > 0 && cam.crop_h > 0;
+    RenderParams rp{};
+    rp.seed = o->seed;
+    rp.spp = o->spp;
+    rp.max_bounces = o->max_bounces;
+    rp.sppse = std::max(0, o->sppse);
+    rp.mode = o->mode >= 0 ? o->mode : MODE_ALL;
+    rp.jitter = o->sppe >= 0 ? 1 : 0;
+    rp.ddist = o->ddist_coeff;
+    rp.inv_spp = o->spp > 0 ? 1.0f / (float)o->spp : 0.f;
+    rp.out_w = cropped ? cam.crop_w : cam.width;
+    rp.out_h = cropped ? cam.crop_h : cam.height;
+    rp.crop_x = cropped ? cam.crop_x : 0;
+    rp.crop_y = cropped ? cam.crop_y : 0;
+    rp.npix = rp.out_w * rp.out_h;
+    if (o->max_bounces < 0) {
+        set_last_error("max_bounces must be >= 0");
+        return DTRT_ERR_INVALID;
+    }
+    const size_t npix = (size_t)rp.npix;
+    // ---------------------------------------------------------------- buffers
+    const size_t acc1_n = (N + 1) * npix * 3, acc2_n = (size_t)N * npix * 3, out_n = (N + 1) * npix * 3;
+    if (!ensure_buffer((void **)&sb.acc1, &sb.acc1_n, acc1_n * 8) || !ensure_buffer((void **)&sb.acc2, &sb.acc2_n, acc2_n * 8))
+        return DTRT_ERR_CUDA;
+    if (!out_on_device && !ensure_buffer((void **)&sb.out, &sb.out_n, out_n * 4)) return DTRT_ERR_CUDA;
+    const uint64_t li_cap = s->queue_cap ? s->queue_cap : (uint64_t)24 << 20;
+    const uint64_t rec_cap = s->queue_cap ? s->queue_cap : (uint64_t)4 << 20;
+    if (!ensure_buffer(&sb.qli, &sb.qli_bytes, li_cap * sizeof(LiTask<N>)) ||
+        !ensure_buffer(&sb.qe, &sb.qe_bytes, rec_cap * sizeof(EdgeRec<N>)) ||
+        !ensure_buffer(&sb.ql, &sb.ql_bytes, rec_cap * sizeof(LinsRec<N>)))
+        return DTRT_ERR_CUDA;
+    if (!sb.counts) DT_CK(cudaMalloc(&sb.counts, 32 * sizeof(unsigned long long)));
+    if (!sb.err) DT_CK(cudaMalloc(&sb.err, sizeof(unsigned int)));
+    sc.error_flags = sb.err;
+    DT_CK(cudaMemsetAsync(sb.acc1, 0, acc1_n * 8, st));
+    DT_CK(cudaMemsetAsync(sb.acc2, 0, acc2_n * 8, st));
+    DT_CK(cudaMemsetAsync(sb.counts, 0, 32 * sizeof(unsigned long long), st));
+    DT_CK(cudaMemsetAsync(sb.err, 0, sizeof(unsigned int), st));
+    unsigned long long *ctr = s->counters ? sb.counts + 8 : nullptr;
+    Queue qe{sb.qe, sb.counts + 0, rec_cap}, ql{sb.ql, sb.counts + 1, rec_cap}, qli{sb.qli, sb.counts + 2, li_cap};
+
+    cudaEvent_t e0, e1;
+    DT_CK(cudaEventCreate(&e0));
+    DT_CK(cudaEventCreate(&e1));
+    double ms_camera = 0, ms_edge = 0, ms_li = 0, ms_primary = 0;
+    auto timed = [&](double &acc, auto &&launch) -> int {
+        cudaEventRecord(e0, st);
+        launch();
+        cudaEventRecord(e1, st);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) {
+            set_last_error(std::string("kernel launch: ") + cudaGetErrorString(err));
+            return DTRT_ERR_CUDA;
+        }
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        acc += ms;
+        return DTRT_OK;
+    };
+    unsigned long long hcnt[3];
+    auto read_counts = [&]() -> int {
+        DT_CK(cudaMemcpyAsync(hcnt, sb.counts, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        DT_CK(cudaStreamSynchronize(st));
+        return DTRT_OK;
+    };
+    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
+    uint64_t tot_edge = 0, tot_lins = 0, tot_li = 0, batches = 0;
+    int rc = DTRT_OK;
+    // Li tasks are drained chunk by chunk so that the queue never exceeds li_cap
+    auto drain_li = [&]() -> int {
+        if ((rc = read_counts())) return rc;
+        const unsigned long long n = std::min<unsigned long long>(hcnt[2], li_cap);
+        tot_li += n;
+        if (n)
+            if ((rc = timed(ms_li, [&] { k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, sb.acc1, sb.acc2, ctr); })))
+                return rc;
+        DT_CK(cudaMemsetAsync(sb.counts + 2, 0, sizeof(unsigned long long), st));
+        return DTRT_OK;
+    };
+
+    // ---------------------------------------------------------------- pass 1
+    const long long total = (long long)npix * std::max(0, o->spp);
+    if (total > 0) {
+        const long long unit = std::max<long long>(128, (long long)rp.spp % 32 == 0 ? std::max(rp.spp, 128) : 128);
+        long long B = (long long)(rec_cap / (uint64_t)std::max(1, o->max_bounces + 1));
+        B = std::max<long long>(unit, (B / unit) * unit);
+        const long long per_chunk = std::max<long long>(1, (long long)(li_cap / (uint64_t)std::max(1, 2 * rp.sppse)));
+        for (long long b0 = 0; b0 < total; b0 += B) {
+            ++batches;
+            rp.path_begin = b0;
+            rp.path_count = std::min(B, total - b0);
+            DT_CK(cudaMemsetAsync(sb.counts, 0, 3 * sizeof(unsigned long long), st));
+            if ((rc = timed(ms_camera, [&] {
+                     k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
+                 })))
+                return rc;
+            if ((rc = read_counts())) return rc;
+            const unsigned long long ne = std::min<unsigned long long>(hcnt[0], rec_cap);
+            const unsigned long long nl = std::min<unsigned long long>(hcnt[1], rec_cap);
+            tot_edge += ne;
+            tot_lins += nl;
+            for (unsigned long long r0 = 0; r0 < ne && rp.sppse > 0; r0 += per_chunk) {
+                const long long cnt = (long long)std::min<unsigned long long>(per_chunk, ne - r0);
+                if ((rc = timed(ms_edge, [&] {
+                         k_edge<N><<<blocks(cnt * rp.sppse), kBlock, 0, st>>>(sc, rp, qe, (long long)r0, cnt, qli, ctr);
+                     })))
+                    return rc;
+                if ((rc = drain_li())) return rc;
+            }
+            if (nl)
+                if ((rc = timed(ms_li, [&] { k_lins<N><<<blocks(nl), kBlock, 0, st>>>(sc, rp, ql, nl, sb.acc1, ctr); })))
+                    return rc;
+        }
+    }
+    // ---------------------------------------------------------------- pass 2: primary edges
+    uint64_t prim_samples = 0;
+    if (o->sppe > 0 && sc.num_pedges > 0) {
+        const long long nblock = (long long)std::ceil(sc.pedge_sum * o->sppe / 128.0);
+        const long long ns = nblock * 128;
+        prim_samples = (uint64_t)ns;
+        rp.prim_weight = sc.pedge_sum / (double)ns;
+        const long long chunk = std::max<long long>(1, (long long)(li_cap / 2));
+        for (long long k0 = 0; k0 < ns; k0 += chunk) {
+            rp.prim_begin = k0;
+            rp.prim_count = std::min(chunk, ns - k0);
+            if ((rc = timed(ms_primary, [&] {
+                     k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, ctr);
+                 })))
+                return rc;
+            if ((rc = drain_li())) return rc;
+        }
+    }
+    // ---------------------------------------------------------------- finalize
+    float *dst = out_on_device ? out : sb.out;
+    k_finalize<N><<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(rp, sb.acc1, sb.acc2, dst);
+    DT_CK(cudaGetLastError());
+    if (!out_on_device) DT_CK(cudaMemcpyAsync(out, sb.out, out_n * 4, cudaMemcpyDeviceToHost, st));
+    unsigned int herr = 0;
+    unsigned long long hc[CT_NUM] = {0};
+    DT_CK(cudaMemcpyAsync(&herr, sb.err, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    if (ctr) DT_CK(cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    DT_CK(cudaStreamSynchronize(st));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dtrt_render_stats &ls = s->last;
+    std::memset(&ls, 0, sizeof(ls));
+    ls.camera_paths = (uint64_t)total;
+    ls.edge_records = tot_edge;
+    ls.lins_records = tot_lins;
+    ls.li_tasks = tot_li;
+    ls.primary_edge_samples = prim_samples;
+    ls.batches = batches;
+    ls.counters_enabled = ctr != nullptr;
+    ls.rays = hc[CT_RAYS];
+    ls.node_visits = hc[CT_NODES];
+    ls.tri_tests = hc[CT_TRIS];
+    ls.grid_lookups = hc[CT_LOOKUPS];
+    ls.edge_samples = ctr ? hc[CT_EDGE_SAMPLES] : tot_edge * (uint64_t)rp.sppse;
+    ls.ms_camera = ms_camera;
+    ls.ms_edge = ms_edge;
+    ls.ms_li = ms_li;
+    ls.ms_primary = ms_primary;
+    ls.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
+    if (herr & ERR_QUEUE) {
+        set_last_error("work queue overflow (capacity below one camera path's worst case)");
+        return DTRT_ERR_OVERFLOW;
+    }
+    if (herr & ERR_STACK) {
+        set_last_error("BVH traversal stack overflow");
+        return DTRT_ERR_INVALID;
+    }
+    if (herr & ERR_TRACK_CAP) {
+        set_last_error("a delta/ratio tracking loop hit its iteration cap");
+        return DTRT_ERR_STEP_CAP;
+    }
+    return DTRT_OK;
+}
+
+}  // namespace dt

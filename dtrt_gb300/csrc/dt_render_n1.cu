@@ -1,0 +1,6 @@
+// dtrt_gb300 — render kernels and orchestration instantiated for nder = 1.
+#include "dt_render.cuh"
+
+namespace dt {
+template int render_n<1>(dtrt_scene *, const dtrt_render_options *, float *, int, cudaStream_t);
+}

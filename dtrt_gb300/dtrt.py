@@ -1,0 +1,356 @@
+"""Drop-in replacement for the reference's native module `dtrt` (src/dtrt.cpp:24-155).
+
+Every class and constructor overload of the pybind module exists here with the same
+argument order and meaning. Constructors copy their inputs from the raw addresses
+they are given (float_ptr / int_ptr wrap `tensor.data_ptr()` of CPU tensors), as the
+reference's constructors do (src/shape.cpp:14-31, src/camera.cpp:13-27); `Scene`
+uploads everything to the GPU through the C ABI and `VolPathTracerAD.render` runs the
+CUDA path tracer.
+
+`nder` (derivative images per render) is read from the DTRT_NDER environment variable
+at import (default 4, the reference's compile-time constant, include/config.h:5) and can
+be changed with set_nder() to any of 1, 3, 4, 8.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi
+
+nder = int(os.environ.get("DTRT_NDER", "4"))
+angleEps = float(np.float32(1e-4))  # config.h:7 (float literal)
+
+
+def set_nder(n):
+    """Select the derivative width for scenes built afterwards (1, 3, 4 or 8)."""
+    global nder
+    if n not in (1, 3, 4, 8):
+        raise ValueError("nder must be 1, 3, 4 or 8")
+    nder = int(n)
+    from . import pydtrt
+    pydtrt._sync_nder(nder)
+
+
+if nder not in (1, 3, 4, 8):
+    raise ImportError("DTRT_NDER must be 1, 3, 4 or 8")
+
+
+class _Ptr:
+    __slots__ = ("addr",)
+
+    def __init__(self, addr=0):
+        self.addr = int(addr)
+
+    def is_null(self):
+        return self.addr == 0
+
+
+class float_ptr(_Ptr):
+    """Raw float* address (ptr<float>, include/ptr.h)."""
+
+
+class int_ptr(_Ptr):
+    """Raw int* address (ptr<int>)."""
+
+
+def _addr(p):
+    if p is None:
+        return 0
+    if isinstance(p, _Ptr):
+        return p.addr
+    return int(p)
+
+
+def _read(p, n, ctype=ctypes.c_float, dtype=np.float32):
+    a = _addr(p)
+    if a == 0:
+        return None
+    return np.frombuffer((ctype * n).from_address(a), dtype=dtype).copy()
+
+
+class Spectrum3f:
+    def __init__(self, r, g, b):
+        self.v = np.array([r, g, b], np.float32)
+
+
+# --------------------------------------------------------------------------- scene objects
+class Camera:
+    """Camera(width, height, cam_to_world*, cam_to_ndc*, clip_near, med_id, velocities*)."""
+
+    def __init__(self, width, height, cam_to_world, cam_to_ndc, clip_near, med_id, velocities=0):
+        self.width, self.height = int(width), int(height)
+        self.cam_to_world = _read(cam_to_world, 16)
+        self.cam_to_ndc = _read(cam_to_ndc, 9)
+        if abs(self.cam_to_ndc[0] - self.cam_to_ndc[4]) > 0:
+            raise ValueError("cam_to_ndc(0,0) must equal cam_to_ndc(1,1) (camera.cpp:21)")
+        self.clip_near = float(clip_near)
+        self.med_id = int(med_id)
+        self.velocities = _read(velocities, 6 * nder)
+        self.rect = (0, 0, -1, -1)
+        self._nder = nder
+
+    def set_rect(self, offset_x, offset_y, crop_width, crop_height):
+        self.rect = (int(offset_x), int(offset_y), int(crop_width), int(crop_height))
+
+
+class Shape:
+    """Shape(V*, F*, UV*, N*, nV, nT, light_id, bsdf_id, med_int_id, med_ext_id, velocities*)."""
+
+    def __init__(self, vertices, indices, uvs, normals, num_vertices, num_triangles, light_id, bsdf_id,
+                 med_int_id, med_ext_id, velocities=0):
+        nv, nt = int(num_vertices), int(num_triangles)
+        self.vertices = _read(vertices, 3 * nv).reshape(nv, 3)
+        self.indices = _read(indices, 3 * nt, ctypes.c_int, np.int32).reshape(nt, 3)
+        uv = _read(uvs, 2 * nv)
+        self.uvs = uv.reshape(nv, 2) if uv is not None else None
+        nrm = _read(normals, 3 * nv)
+        self.normals = nrm.reshape(nv, 3) if nrm is not None else None
+        nvel = nder * nv * 3 * (2 if self.normals is not None else 1)
+        vel = _read(velocities, nvel)
+        self.velocities = vel.reshape(-1, 3) if vel is not None else None
+        self.num_vertices, self.num_triangles = nv, nt
+        self.light_id, self.bsdf_id = int(light_id), int(bsdf_id)
+        self.med_int_id, self.med_ext_id = int(med_int_id), int(med_ext_id)
+
+    def has_uvs(self):
+        return self.uvs is not None
+
+    def has_normals(self):
+        return self.normals is not None
+
+
+class BSDF:
+    pass
+
+
+class BSDF_diffuse(BSDF):
+    def __init__(self, reflectance, d_reflectance=None):
+        self.type = _abi.BSDF_DIFFUSE
+        self.diffuse = reflectance.v
+        self.d_diffuse = _read(d_reflectance, 3 * nder)
+
+
+class BSDF_null(BSDF):
+    def __init__(self):
+        self.type = _abi.BSDF_NULL
+
+
+class BSDF_Phong(BSDF):
+    def __init__(self, diffuse, specular, exponent, d_diffuse=None, d_specular=None, d_exponent=None):
+        self.type = _abi.BSDF_PHONG
+        self.diffuse, self.specular, self.exponent = diffuse.v, specular.v, float(exponent)
+        self.d_diffuse = _read(d_diffuse, 3 * nder)
+        self.d_specular = _read(d_specular, 3 * nder)
+        self.d_exponent = _read(d_exponent, nder)
+
+
+class BSDF_roughdielectric(BSDF):
+    def __init__(self, alpha, int_ior, ext_ior, d_alpha=None, d_eta=None):
+        self.type = _abi.BSDF_ROUGHDIELECTRIC
+        self.alpha, self.int_ior, self.ext_ior = float(alpha), float(int_ior), float(ext_ior)
+        self.d_alpha = _read(d_alpha, nder)
+        self.d_eta = _read(d_eta, nder)
+
+
+class Phase:
+    pass
+
+
+class HG(Phase):
+    def __init__(self, g, d_g=None):
+        self.type = _abi.PHASE_HG
+        self.g = float(g)
+        self.d_g = _read(d_g, nder)
+
+
+class Isotropic(Phase):
+    def __init__(self):
+        self.type = _abi.PHASE_ISOTROPIC
+        self.g = 0.0
+        self.d_g = None
+
+
+class Emitter:
+    pass
+
+
+class AreaLight(Emitter):
+    """AreaLight(shape_id, intensity*, two_sided) (area.h:13-18)."""
+
+    def __init__(self, shape_id, intensity, two_sided=False):
+        self.type = _abi.EMITTER_AREA
+        self.shape_id = int(shape_id)
+        self.intensity = _read(intensity, 3)
+        self.two_sided = bool(two_sided)
+        self.kappa, self.d_intensity, self.d_kappa = 0.0, None, None
+
+
+class AreaLightEx(Emitter):
+    """AreaLightEx(shape_id, Spectrum3f intensity, kappa[, dI*, dKappa*]) (area2.h:11-17)."""
+
+    def __init__(self, shape_id, intensity, kappa, d_intensity=None, d_kappa=None):
+        self.type = _abi.EMITTER_AREA_EX
+        self.shape_id = int(shape_id)
+        self.intensity = intensity.v
+        self.kappa = float(kappa)
+        self.two_sided = False
+        self.d_intensity = _read(d_intensity, 3 * nder)
+        self.d_kappa = _read(d_kappa, nder)
+
+
+class Medium:
+    pass
+
+
+class Homogeneous(Medium):
+    def __init__(self, sigma_t, albedo, phase_id, d_sigma_t=None, d_albedo=None):
+        self.type = _abi.MEDIUM_HOMOGENEOUS
+        self.sigma_t, self.albedo, self.phase_id = float(sigma_t), albedo.v, int(phase_id)
+        self.d_sigma_t = _read(d_sigma_t, nder)
+        self.d_albedo = _read(d_albedo, 3 * nder)
+
+
+class Heterogeneous(Medium):
+    """Heterogeneous(file, toWorld*, scale, albedo (Spectrum3f | albedo file), phase_id
+    [, trans_vel*, rot_vel*, d_scale*[, d_albedo*]]) (heterogeneous.h:28-75)."""
+
+    def __init__(self, density_file, to_world, scale, albedo, phase_id, trans_velocities=None,
+                 rot_velocities=None, d_scale=None, d_albedo=None):
+        self.type = _abi.MEDIUM_HETEROGENEOUS
+        self.density_file = str(density_file)
+        self.to_world = _read(to_world, 16)
+        self.scale = float(scale)
+        if isinstance(albedo, str):
+            self.albedo_file, self.albedo = albedo, np.zeros(3, np.float32)
+        else:
+            self.albedo_file, self.albedo = None, albedo.v
+        self.phase_id = int(phase_id)
+        self.trans_velocities = _read(trans_velocities, 3 * nder)
+        self.rot_velocities = _read(rot_velocities, 3 * nder)
+        self.d_scale = _read(d_scale, nder)
+        self.d_albedo = _read(d_albedo, 3 * nder) if self.albedo_file is None else None
+
+
+class Scene:
+    """Scene(camera, shapes, bsdfs, emitters, phases, media) (scene.cpp:9-136): the
+    device scene (BVH, light and edge distributions) is built here."""
+
+    def __init__(self, camera, shapes, bsdfs, emitters, phases, media):
+        from . import scenes as S
+        self._nder = camera._nder
+        cam = S.CameraSpec(camera.width, camera.height, camera.cam_to_world.reshape(4, 4),
+                           camera.cam_to_ndc.reshape(3, 3), camera.clip_near, camera.med_id,
+                           camera.velocities.reshape(-1, 3) if camera.velocities is not None else None, camera.rect)
+        spec = S.SceneSpec(self._nder, cam, [], [])
+        for s in shapes:
+            spec.shapes.append(S.ShapeSpec(s.vertices, s.indices, s.bsdf_id, s.light_id, s.med_int_id, s.med_ext_id,
+                                           s.normals, s.uvs, s.velocities))
+        for b in bsdfs:
+            spec.bsdfs.append(S.BsdfSpec(b.type, diffuse=tuple(getattr(b, "diffuse", (0, 0, 0))),
+                                         specular=tuple(getattr(b, "specular", (0, 0, 0))),
+                                         exponent=getattr(b, "exponent", 0.0), alpha=getattr(b, "alpha", 0.1),
+                                         int_ior=getattr(b, "int_ior", 1.5), ext_ior=getattr(b, "ext_ior", 1.0),
+                                         d_diffuse=getattr(b, "d_diffuse", None),
+                                         d_specular=getattr(b, "d_specular", None),
+                                         d_exponent=getattr(b, "d_exponent", None),
+                                         d_alpha=getattr(b, "d_alpha", None), d_eta=getattr(b, "d_eta", None)))
+        for e in emitters:
+            spec.emitters.append(S.EmitterSpec(e.shape_id, tuple(e.intensity), e.type, e.two_sided, e.kappa,
+                                               e.d_intensity, e.d_kappa))
+        for p in phases:
+            spec.phases.append(S.PhaseSpec(p.type, p.g, p.d_g))
+        for m in media:
+            if m.type == _abi.MEDIUM_HOMOGENEOUS:
+                spec.media.append(S.MediumSpec(m.type, m.phase_id, m.sigma_t, tuple(m.albedo), m.d_sigma_t, m.d_albedo))
+            else:
+                spec.media.append(S.MediumSpec(m.type, m.phase_id, albedo=tuple(m.albedo), d_albedo=m.d_albedo,
+                                               density_file=m.density_file, albedo_file=m.albedo_file,
+                                               to_world=m.to_world.reshape(4, 4), density_scale=m.scale,
+                                               d_density_scale=m.d_scale, trans_velocities=m.trans_velocities,
+                                               rot_velocities=m.rot_velocities))
+        self.spec = spec
+        from .native import NativeScene
+        self.native = NativeScene(spec)
+
+    def initEdges(self, weights):
+        """Secondary-edge sampling weight per shape (scene.h:37-39)."""
+        w = _read(weights, len(self.spec.shapes))
+        self.native.set_edge_weights(w)
+
+    def close(self):
+        self.native.close()
+
+
+class RenderOptions:
+    """RenderOptions(seed, spp, max_bounces, sppe, sppse, quiet[, mode[, ddistCoeff]])."""
+
+    def __init__(self, seed, spp, max_bounces, sppe, sppse, quiet, mode=-1, ddistCoeff=0.0):
+        self.seed, self.spp, self.max_bounces = int(seed), int(spp), int(max_bounces)
+        self.sppe, self.sppse, self.quiet = int(sppe), int(sppse), bool(quiet)
+        self.mode, self.ddistCoeff = int(mode), float(ddistCoeff)
+
+    def _c(self):
+        return _abi.RenderOptions(self.seed & ((1 << 64) - 1), self.spp, self.max_bounces, self.sppe, self.sppse,
+                                  int(self.quiet), self.mode, self.ddistCoeff)
+
+
+class Integrator:
+    name = "Integrator"
+
+    def render(self, scene, options, rendered_image):
+        raise NotImplementedError(f"{self.name} is not provided by dtrt_gb300 (only VolPathTracerAD and "
+                                  "VolPathTracer render)")
+
+
+class VolPathTracerAD(Integrator):
+    """Forward-mode volumetric path tracer (volpathAD.cpp) on the GPU: writes the image
+    and nder derivative images into the float[(nder+1)][H][W][3] buffer at `rendered_image`."""
+    name = "VolPathTracerAD"
+
+    def render(self, scene, options, rendered_image):
+        lib = _abi.load()
+        o = options._c()
+        _abi.check(lib.dtrt_render_fwd(scene.native.handle, ctypes.byref(o), ctypes.c_void_p(_addr(rendered_image)),
+                                       0, None))
+
+
+class VolPathTracer(Integrator):
+    """Primal volumetric path tracer: the value part of the forward-mode estimator
+    (same expectation as volpath.cpp's radiance), written to slot 0 only."""
+    name = "VolPathTracer"
+
+    def render(self, scene, options, rendered_image):
+        spec = scene.spec
+        buf = np.zeros(spec.out_shape(), np.float32)
+        o = options._c()
+        o.sppse, o.sppe = 0, 0
+        lib = _abi.load()
+        _abi.check(lib.dtrt_render_fwd(scene.native.handle, ctypes.byref(o), buf.ctypes.data_as(ctypes.c_void_p), 0, None))
+        n = buf[0].size
+        dst = (ctypes.c_float * n).from_address(_addr(rendered_image))
+        ctypes.memmove(dst, buf[0].ctypes.data, n * 4)
+
+
+class DirectIntegrator(Integrator):
+    name = "DirectIntegrator"
+
+
+class PathTracer(Integrator):
+    name = "PathTracer"
+
+
+class ParticleTracer(Integrator):
+    name = "ParticleTracer"
+
+
+class VolPathTracerSimple(Integrator):
+    name = "VolPathTracerSimple"
+
+
+class DirectAD(Integrator):
+    name = "DirectAD"
+
+
+class PathTracerAD(Integrator):
+    name = "PathTracerAD"

@@ -1,0 +1,145 @@
+"""Known-answer tests pinning the FP64 CPU oracle (no GPU). The reference ships no
+tests or golden vectors, so the oracle is pinned by published PCG32 outputs,
+closed-form identities and an analytic direct-lighting integral."""
+import math
+
+import numpy as np
+import pytest
+
+from dtrt_gb300 import _abi, scenes
+from dtrt_gb300.scenes import BsdfSpec, CameraSpec, EmitterSpec, SceneSpec, ShapeSpec
+
+
+def test_pcg32_published_outputs(oracle):
+    # RndSampler(seed, idx) == pcg32_srandom(0x853c49e6748fea9b + seed, idx + 1); the
+    # PCG32 reference demo (initstate 42, initseq 54) prints these six values.
+    seed = (42 - 0x853C49E6748FEA9B) % (1 << 64)
+    got = oracle.pcg32(seed, 53, 6)
+    assert [hex(int(x)) for x in got] == ["0xa15c02b7", "0x7b47f409", "0xba1d3330", "0x83d2f293", "0xbfa4784b",
+                                          "0xcbed606e"]
+
+
+def test_golden_rng_fixture(oracle):
+    import json
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "pcg32.json")
+    data = json.load(open(path))
+    for case in data["cases"]:
+        u32 = oracle.pcg32(case["seed"], case["idx"], len(case["u32"]))
+        assert [int(x) for x in u32] == case["u32"]
+        u = oracle.next1d(case["seed"], case["idx"], len(case["u32"]))
+        assert np.allclose(u, np.array(case["u32"], dtype=np.float64) / 2.0 ** 32, rtol=0, atol=2.0 ** -52)
+
+
+def test_uniform_range_and_mean(oracle):
+    u = oracle.next1d(7, 3, 200000)
+    assert u.min() >= 0.0 and u.max() < 1.0
+    assert abs(u.mean() - 0.5) < 0.005
+
+
+@pytest.mark.parametrize("eta", [1.33, 1.5, 2.0])
+def test_fresnel_normal_incidence(oracle, eta):
+    assert oracle.closed_form(0, 1.0, eta) == pytest.approx(((eta - 1) / (eta + 1)) ** 2, rel=1e-12)
+    assert oracle.closed_form(0, 0.3, 1.0) == 0.0
+    # total internal reflection from the dense side beyond the critical angle
+    assert oracle.closed_form(0, -0.1, 1.5) == 1.0
+
+
+@pytest.mark.parametrize("g", [-0.5, 0.0, 0.3, 0.8])
+def test_hg_normalised(oracle, g):
+    mu = np.linspace(-1, 1, 200001)
+    p = np.array([oracle.closed_form(1, g, m) for m in mu[::100]])
+    integral = 2 * math.pi * np.trapezoid(p, mu[::100])
+    assert integral == pytest.approx(1.0, abs=2e-3)
+
+
+@pytest.mark.parametrize("alpha", [0.05, 0.2, 0.6])
+def test_beckmann_projected_area_is_one(oracle, alpha):
+    ct = np.linspace(1e-6, 1.0, 20001)
+    d = np.array([oracle.closed_form(2, alpha, c) for c in ct])
+    integral = 2 * math.pi * np.trapezoid(d * ct, ct)  # int D(m) cos(theta_m) dw_m
+    assert integral == pytest.approx(1.0, rel=2e-3)
+
+
+def test_smith_g1_limits(oracle):
+    assert oracle.closed_form(3, 0.3, 1.0) == 1.0  # normal incidence: no masking
+    assert oracle.closed_form(3, 0.3, 0.05) < 0.5  # grazing
+
+
+def test_erf_approximations(oracle):
+    for x in np.linspace(-3, 3, 61):
+        assert oracle.closed_form(4, x) == pytest.approx(math.erf(x), abs=2e-7)
+    for y in np.linspace(-0.99, 0.99, 41):
+        assert math.erf(oracle.closed_form(5, y)) == pytest.approx(y, abs=2e-6)
+
+
+def test_bsdf_sampling_weights(oracle):
+    alb = oracle.bsdf_albedo(BsdfSpec(_abi.BSDF_DIFFUSE, diffuse=(0.25, 0.5, 0.75)), 0.7)
+    assert np.allclose(alb, [0.25, 0.5, 0.75], rtol=1e-12)
+    ph = oracle.bsdf_albedo(BsdfSpec(_abi.BSDF_PHONG, diffuse=(0.3, 0.3, 0.3), specular=(0.2, 0.2, 0.2),
+                                     exponent=20.0), 0.8, nsamples=400000)
+    assert 0.35 < ph[0] < 0.52  # energy of a modified Phong lobe below kd + ks
+    rd = oracle.bsdf_albedo(BsdfSpec(_abi.BSDF_ROUGHDIELECTRIC, alpha=0.2, int_ior=1.5, ext_ior=1.0), 0.9,
+                            nsamples=400000)
+    # radiance scaling by 1/eta^2 on refraction into the dense side (roughdielectric.cpp:218-223)
+    assert 0.40 < rd[0] < 0.50
+
+
+def _direct_light_scene(width=4, height=4):
+    """Camera looking down at a diffuse ground under a 1x1 light; no other geometry."""
+    shapes, bsdfs, emitters = [], [], []
+    scenes._stage(shapes, bsdfs, emitters, ground_albedo=0.5)
+    cam = scenes._camera(width, height, fov_deg=20.0, pos=(0.3, 1.5, 0.9), target=(0.3, -1.0, 0.2),
+                         up=(0.0, 0.0, -1.0))
+    return SceneSpec(1, cam, shapes, bsdfs, emitters, [], [], name="direct")
+
+
+def _analytic_direct(spec, px, py):
+    """rho/pi * int_light L cos_x cos_l / r^2 dA for the pixel-centre ray."""
+    c2w = spec.camera.cam_to_world.astype(np.float64)
+    ndc2cam = np.linalg.inv(spec.camera.cam_to_ndc.astype(np.float64))
+    w, h = spec.camera.width, spec.camera.height
+    x, y = (px + 0.5) / w, (py + 0.5) / h
+    d = ndc2cam @ np.array([(x - 0.5) * 2, (y - 0.5) * -2 / (w / h), 1.0])
+    d = c2w[:3, :3] @ (d / np.linalg.norm(d))
+    o = c2w[:3, 3]
+    t = (-1.0 - o[1]) / d[1]
+    p = o + t * d
+    n = 2000
+    g = (np.arange(n) + 0.5) / n - 0.5
+    lx, lz = np.meshgrid(g, g)
+    q = np.stack([lx.ravel(), np.full(lx.size, 2.0), lz.ravel()], 1)
+    v = q - p
+    r2 = (v * v).sum(1)
+    cos_x = v[:, 1] / np.sqrt(r2)
+    cos_l = v[:, 1] / np.sqrt(r2)  # light normal (0,-1,0) dotted with -v/|v|
+    E = (10.0 * cos_x * cos_l / r2).sum() * (1.0 / n) ** 2
+    return 0.5 / math.pi * E
+
+
+def test_direct_lighting_matches_analytic_integral(oracle):
+    spec = _direct_light_scene()
+    img = oracle.render(spec, seed=3, spp=4096, max_bounces=1, sppe=-1, sppse=0)
+    for px, py in [(0, 0), (1, 2), (3, 3)]:
+        ref = _analytic_direct(spec, px, py)
+        assert img[0, py, px, 0] == pytest.approx(ref, rel=0.01)
+
+
+def test_translation_derivative_matches_finite_difference(oracle):
+    """Total-image derivative of a translating diffuse sphere (interior + edge + primary
+    edge terms) against central differences with common random numbers."""
+    def scene(dx):
+        spec = scenes.config2(16, 16, subdiv=2, nder=1)
+        spec.shapes[0].vertices = (spec.shapes[0].vertices + np.array([dx, 0, 0], np.float32)).astype(np.float32)
+        spec.shapes[0].velocities = np.tile(np.array([[1.0, 0, 0]], np.float32), (spec.shapes[0].vertices.shape[0], 1))
+        return spec
+    kw = dict(spp=64, max_bounces=2, sppe=64, sppse=2)
+    h = 0.02
+    der, fd = [], []
+    for seed in range(4):
+        der.append(oracle.render(scene(0.0), seed=seed, **kw)[1].sum())
+        fd.append((oracle.render(scene(h), seed=seed, **kw)[0].sum() - oracle.render(scene(-h), seed=seed, **kw)[0].sum())
+                  / (2 * h))
+    der, fd = np.array(der), np.array(fd)
+    se = math.sqrt(der.var(ddof=1) / len(der) + fd.var(ddof=1) / len(fd))
+    assert abs(der.mean() - fd.mean()) < 4 * se + 0.05 * abs(fd.mean()), (der, fd)

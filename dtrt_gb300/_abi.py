@@ -117,13 +117,20 @@ class RenderStats(ctypes.Structure):
         ("lins_records", ctypes.c_uint64), ("primary_edge_samples", ctypes.c_uint64),
         ("li_tasks", ctypes.c_uint64), ("rays", ctypes.c_uint64), ("node_visits", ctypes.c_uint64),
         ("tri_tests", ctypes.c_uint64), ("grid_lookups", ctypes.c_uint64), ("batches", ctypes.c_uint64),
+        ("kernel_launches", ctypes.c_uint64),
+        ("k_rays", ctypes.c_uint64 * 5), ("k_node_visits", ctypes.c_uint64 * 5),
+        ("k_tri_tests", ctypes.c_uint64 * 5), ("k_grid_lookups", ctypes.c_uint64 * 5),
         ("ms_total", ctypes.c_double), ("ms_camera", ctypes.c_double), ("ms_edge", ctypes.c_double),
         ("ms_li", ctypes.c_double), ("ms_primary", ctypes.c_double), ("ms_setup", ctypes.c_double),
         ("counters_enabled", ctypes.c_int),
     ]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if isinstance(v, ctypes.Array) else v
+        return d
 
 
 # Every C-ABI symbol declared in include/dtrt_gb300.h, with its ctypes signature.

@@ -65,23 +65,28 @@ struct Queue {
     unsigned long long cap;
 };
 
-// Counter slots (dtrt_render_stats order)
-enum { CT_RAYS = 0, CT_NODES, CT_TRIS, CT_LOOKUPS, CT_EDGE_SAMPLES, CT_LI, CT_PRIMARY, CT_NUM };
+// Counter slots: [kernel][rays, nodes, tris, lookups] then three task counts
+enum { K_CAMERA = 0, K_EDGE, K_LI, K_LINS, K_PRIMARY };
+enum { CT_EDGE_SAMPLES = 20, CT_LI, CT_PRIMARY, CT_NUM };
 
-DT_D void flush_counters(unsigned long long *ctr, const Ctr &c, uint32_t extra_slot = 0xffffffffu, uint32_t extra = 0) {
+DT_D void flush_counters(unsigned long long *ctr, int kernel, const Ctr &c, uint32_t extra_slot = 0xffffffffu,
+                         uint32_t extra = 0) {
     if (!ctr) return;
     unsigned long long v[4] = {c.rays, c.nodes, c.tris, c.lookups};
     const unsigned mask = __activemask();
+    bool lead = true;
+    if (mask == 0xffffffffu) {  // full warp: reduce with shuffles, one atomic per counter
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        unsigned long long x = v[k];
-        for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(mask, x, off);
-        v[k] = x;
+        for (int k = 0; k < 4; ++k) {
+            unsigned long long x = v[k];
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(mask, x, off);
+            v[k] = x;
+        }
+        lead = (threadIdx.x & 31) == 0;
     }
-    if ((threadIdx.x & 31) == (__ffs(mask) - 1)) {
+    if (lead)
         for (int k = 0; k < 4; ++k)
-            if (v[k]) atomicAdd(ctr + k, v[k]);
-    }
+            if (v[k]) atomicAdd(ctr + 4 * kernel + k, v[k]);
     if (extra_slot != 0xffffffffu && extra) atomicAdd(ctr + extra_slot, (unsigned long long)extra);
 }
 
@@ -344,7 +349,7 @@ __global__ void __launch_bounds__(kBlock) k_camera(DevScene sc, RenderParams rp,
             if (vals[k] != 0.f) atomicAdd(acc1 + ((size_t)(k / 3) * rp.npix + pixel) * 3 + (k % 3), (double)vals[k]);
         }
     }
-    if (ctr) flush_counters(ctr, c);
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
 // ====================================================================== FP64 edge geometry
@@ -508,7 +513,7 @@ __global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Q
             }
         }
     }
-    if (ctr) flush_counters(ctr, c, CT_EDGE_SAMPLES, nsamples);
+    if (ctr) flush_counters(ctr, K_EDGE, c, CT_EDGE_SAMPLES, nsamples);
 }
 
 // ====================================================================== Li sub-paths
@@ -540,7 +545,7 @@ __global__ void __launch_bounds__(kBlock) k_li(DevScene sc, RenderParams rp, Que
             }
         }
     }
-    if (ctr) flush_counters(ctr, c, CT_LI, n);
+    if (ctr) flush_counters(ctr, K_LI, c, CT_LI, n);
 }
 
 // ====================================================================== Lins records
@@ -647,7 +652,7 @@ __global__ void __launch_bounds__(kBlock) k_lins(DevScene sc, RenderParams rp, Q
             }
         }
     }
-    if (ctr) flush_counters(ctr, c);
+    if (ctr) flush_counters(ctr, K_LINS, c);
 }
 
 // ====================================================================== primary edges
@@ -725,7 +730,7 @@ __global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp
             }
         }
     }
-    if (ctr) flush_counters(ctr, c, CT_PRIMARY, n);
+    if (ctr) flush_counters(ctr, K_PRIMARY, c, CT_PRIMARY, n);
 }
 
 // ====================================================================== finalize

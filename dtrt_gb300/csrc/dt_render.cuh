@@ -79,7 +79,9 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     DT_CK(cudaEventCreate(&e0));
     DT_CK(cudaEventCreate(&e1));
     double ms_camera = 0, ms_edge = 0, ms_li = 0, ms_primary = 0;
+    uint64_t launches = 0;
     auto timed = [&](double &acc, auto &&launch) -> int {
+        ++launches;
         cudaEventRecord(e0, st);
         launch();
         cudaEventRecord(e1, st);
@@ -170,6 +172,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     // ---------------------------------------------------------------- finalize
     float *dst = out_on_device ? out : sb.out;
     k_finalize<N><<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(rp, sb.acc1, sb.acc2, dst);
+    ++launches;
     DT_CK(cudaGetLastError());
     if (!out_on_device) DT_CK(cudaMemcpyAsync(out, sb.out, out_n * 4, cudaMemcpyDeviceToHost, st));
     unsigned int herr = 0;
@@ -187,11 +190,18 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     ls.li_tasks = tot_li;
     ls.primary_edge_samples = prim_samples;
     ls.batches = batches;
+    ls.kernel_launches = launches;
     ls.counters_enabled = ctr != nullptr;
-    ls.rays = hc[CT_RAYS];
-    ls.node_visits = hc[CT_NODES];
-    ls.tri_tests = hc[CT_TRIS];
-    ls.grid_lookups = hc[CT_LOOKUPS];
+    for (int k = 0; k < 5; ++k) {
+        ls.k_rays[k] = hc[4 * k];
+        ls.k_node_visits[k] = hc[4 * k + 1];
+        ls.k_tri_tests[k] = hc[4 * k + 2];
+        ls.k_grid_lookups[k] = hc[4 * k + 3];
+        ls.rays += hc[4 * k];
+        ls.node_visits += hc[4 * k + 1];
+        ls.tri_tests += hc[4 * k + 2];
+        ls.grid_lookups += hc[4 * k + 3];
+    }
     ls.edge_samples = ctr ? hc[CT_EDGE_SAMPLES] : tot_edge * (uint64_t)rp.sppse;
     ls.ms_camera = ms_camera;
     ls.ms_edge = ms_edge;

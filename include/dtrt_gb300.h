@@ -180,6 +180,9 @@ typedef struct {
     uint64_t tri_tests;       /* triangles fetched and tested                       */
     uint64_t grid_lookups;    /* trilinear density lookups (8 voxels each)          */
     uint64_t batches;         /* camera-path chunks the render was split into       */
+    uint64_t kernel_launches; /* device kernels launched by the render              */
+    /* per-kernel counters, index: 0 camera, 1 edge, 2 Li, 3 Lins, 4 primary edge */
+    uint64_t k_rays[5], k_node_visits[5], k_tri_tests[5], k_grid_lookups[5];
     double ms_total;
     double ms_camera;         /* camera AD path kernel(s)                           */
     double ms_edge;           /* secondary-edge kernel(s)                           */

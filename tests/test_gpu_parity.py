@@ -78,3 +78,27 @@ def test_c2_mesh_derivative_parity(native, oracle):
     g = gpu_runs(native, spec, range(500, 516), **kw)
     c = cpu_runs(oracle, spec, range(600, 608), **kw)
     print(assert_parity(g, c, label="C2"))
+
+
+def _translating_diffuse_sphere(w, h, subdiv=3):
+    spec = scenes.config2(w, h, subdiv=subdiv, nder=1)
+    nv = spec.shapes[0].vertices.shape[0]
+    spec.shapes[0].velocities = np.tile(np.array([[1.0, 0.0, 0.0]], np.float32), (nv, 1))
+    return spec
+
+
+def test_primary_edge_parity_moving_diffuse_sphere(native, oracle):
+    spec = _translating_diffuse_sphere(32, 32)
+    with native.NativeScene(spec) as s:
+        g = np.stack([s.render(seed=sd, spp=0, max_bounces=3, sppe=256, sppse=0)[1:].copy() for sd in range(16)])
+    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=256, max_bounces=3) for sd in range(8)])
+    assert np.abs(c).sum() > 0 and np.abs(g).sum() > 0
+    print(assert_parity(g, c, label="primary edges (moving sphere)"))
+
+
+def test_full_forward_render_moving_diffuse_sphere(native, oracle):
+    spec = _translating_diffuse_sphere(32, 32)
+    kw = dict(spp=16, max_bounces=3, sppe=64, sppse=4)
+    g = gpu_runs(native, spec, range(700, 716), **kw)
+    c = cpu_runs(oracle, spec, range(800, 808), **kw)
+    print(assert_parity(g, c, label="moving sphere all terms"))

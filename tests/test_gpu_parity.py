@@ -89,9 +89,16 @@ def _translating_diffuse_sphere(w, h, subdiv=3):
 
 def test_primary_edge_parity_moving_diffuse_sphere(native, oracle):
     spec = _translating_diffuse_sphere(32, 32)
+    sppe = 256
+    ne, tl, npe, psum = oracle.edge_summary(spec)
     with native.NativeScene(spec) as s:
-        g = np.stack([s.render(seed=sd, spp=0, max_bounces=3, sppe=256, sppse=0)[1:].copy() for sd in range(16)])
-    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=256, max_bounces=3) for sd in range(8)])
+        g = []
+        for sd in range(48):
+            g.append(s.render(seed=sd, spp=0, max_bounces=3, sppe=sppe, sppse=0)[1:].copy())
+            if sd == 0:  # same projected-edge table: same sample count ceil(PDFsum*sppe/128)*128
+                assert s.last_stats()["primary_edge_samples"] == int(np.ceil(psum * sppe / 128.0)) * 128
+        g = np.stack(g)
+    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=sppe, max_bounces=3) for sd in range(48)])
     assert np.abs(c).sum() > 0 and np.abs(g).sum() > 0
     print(assert_parity(g, c, label="primary edges (moving sphere)"))
 

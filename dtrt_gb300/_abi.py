@@ -144,6 +144,8 @@ _SIGNATURES = {
     "dtrt_scene_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dtrt_render_fwd": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
                                        ctypes.c_int, ctypes.c_void_p]),
+    "dtrt_render_fwd_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
+                                               ctypes.c_int, ctypes.c_void_p]),
     "dtrt_scene_enable_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dtrt_scene_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderStats)]),
     "dtrt_scene_set_queue_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),

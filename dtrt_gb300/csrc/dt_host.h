@@ -42,4 +42,7 @@ namespace dt {
 template <int N>
 int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream);
 bool ensure_buffer(void **ptr, size_t *have, size_t need);
+template <int N>
+int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream,
+                     unsigned char *scratch, size_t scratch_bytes);
 }  // namespace dt

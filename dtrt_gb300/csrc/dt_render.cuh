@@ -224,3 +224,174 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
 }
 
 }  // namespace dt
+
+namespace dt {
+
+// ====================================================================== no-allocation render
+// Same work as render_n, on caller-provided scratch (the static array of dt_noalloc.cu):
+// fixed small queue capacities, no cudaMalloc / cudaFree / event creation.
+constexpr uint64_t kNoallocLiCap = 16384, kNoallocRecCap = 4096;
+
+template <int N>
+int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t st,
+                     unsigned char *scratch, size_t scratch_bytes) {
+    using clk = std::chrono::steady_clock;
+    const auto t_start = clk::now();
+    DevScene sc = s->dev;
+    const DevCamera &cam = sc.cam;
+    const bool cropped = cam.crop_w > 0 && cam.crop_h > 0;
+    RenderParams rp{};
+    rp.seed = o->seed;
+    rp.spp = o->spp;
+    rp.max_bounces = o->max_bounces;
+    rp.sppse = std::max(0, o->sppse);
+    rp.mode = o->mode >= 0 ? o->mode : MODE_ALL;
+    rp.jitter = o->sppe >= 0 ? 1 : 0;
+    rp.ddist = o->ddist_coeff;
+    rp.inv_spp = o->spp > 0 ? 1.0f / (float)o->spp : 0.f;
+    rp.out_w = cropped ? cam.crop_w : cam.width;
+    rp.out_h = cropped ? cam.crop_h : cam.height;
+    rp.crop_x = cropped ? cam.crop_x : 0;
+    rp.crop_y = cropped ? cam.crop_y : 0;
+    rp.npix = rp.out_w * rp.out_h;
+    const size_t npix = (size_t)rp.npix;
+    if (npix > DTRT_NOALLOC_MAX_PIXELS) {
+        set_last_error("dtrt_render_fwd_noalloc: image has " + std::to_string(npix) + " pixels, the maximum is " +
+                       std::to_string(DTRT_NOALLOC_MAX_PIXELS));
+        return DTRT_ERR_INVALID;
+    }
+    if (o->max_bounces < 0 || o->max_bounces > 31 || rp.sppse > (int)(kNoallocLiCap / 2)) {
+        set_last_error("dtrt_render_fwd_noalloc: needs 0 <= max_bounces <= 31 and sppse <= 8192");
+        return DTRT_ERR_INVALID;
+    }
+    // carve the scratch array (256-byte aligned pieces)
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> unsigned char * {
+        unsigned char *p = scratch + off;
+        off += (bytes + 255) & ~(size_t)255;
+        return p;
+    };
+    const size_t acc1_n = (N + 1) * npix * 3, acc2_n = (size_t)N * npix * 3, out_n = (N + 1) * npix * 3;
+    double *acc1 = (double *)take(acc1_n * 8);
+    double *acc2 = (double *)take(acc2_n * 8);
+    float *stage = out_on_device ? nullptr : (float *)take(out_n * 4);
+    unsigned long long *counts = (unsigned long long *)take(32 * sizeof(unsigned long long));
+    unsigned int *err = (unsigned int *)take(sizeof(unsigned int));
+    void *qli_p = take(kNoallocLiCap * sizeof(LiTask<N>));
+    void *qe_p = take(kNoallocRecCap * sizeof(EdgeRec<N>));
+    void *ql_p = take(kNoallocRecCap * sizeof(LinsRec<N>));
+    if (off > scratch_bytes) {
+        set_last_error("dtrt_render_fwd_noalloc: scratch array too small for this image");
+        return DTRT_ERR_INVALID;
+    }
+    sc.error_flags = err;
+    DT_CK(cudaMemsetAsync(acc1, 0, acc1_n * 8, st));
+    DT_CK(cudaMemsetAsync(acc2, 0, acc2_n * 8, st));
+    DT_CK(cudaMemsetAsync(counts, 0, 32 * sizeof(unsigned long long), st));
+    DT_CK(cudaMemsetAsync(err, 0, sizeof(unsigned int), st));
+    Queue qe{qe_p, counts + 0, kNoallocRecCap}, ql{ql_p, counts + 1, kNoallocRecCap}, qli{qli_p, counts + 2, kNoallocLiCap};
+    unsigned long long hcnt[3];
+    uint64_t launches = 0, batches = 0, tot_edge = 0, tot_lins = 0, tot_li = 0;
+    auto read_counts = [&]() -> int {
+        DT_CK(cudaMemcpyAsync(hcnt, counts, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        DT_CK(cudaStreamSynchronize(st));
+        return DTRT_OK;
+    };
+    auto launched = [&]() -> int {
+        ++launches;
+        DT_CK(cudaGetLastError());
+        return DTRT_OK;
+    };
+    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
+    int rc = DTRT_OK;
+    auto drain_li = [&]() -> int {
+        if ((rc = read_counts())) return rc;
+        const unsigned long long n = std::min<unsigned long long>(hcnt[2], kNoallocLiCap);
+        tot_li += n;
+        if (n) {
+            k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, acc1, acc2, nullptr);
+            if ((rc = launched())) return rc;
+        }
+        DT_CK(cudaMemsetAsync(counts + 2, 0, sizeof(unsigned long long), st));
+        return DTRT_OK;
+    };
+    const long long total = (long long)npix * std::max(0, o->spp);
+    if (total > 0) {
+        // 128-path units keep every warp inside one pixel whenever spp is a multiple of 32
+        const long long unit = 128;
+        long long B = (long long)(kNoallocRecCap / (uint64_t)(o->max_bounces + 1));
+        B = std::max<long long>(unit, (B / unit) * unit);
+        const long long per_chunk = std::max<long long>(1, (long long)(kNoallocLiCap / (uint64_t)std::max(1, 2 * rp.sppse)));
+        for (long long b0 = 0; b0 < total; b0 += B) {
+            ++batches;
+            rp.path_begin = b0;
+            rp.path_count = std::min(B, total - b0);
+            DT_CK(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), st));
+            k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, acc1, nullptr);
+            if ((rc = launched())) return rc;
+            if ((rc = read_counts())) return rc;
+            const unsigned long long ne = std::min<unsigned long long>(hcnt[0], kNoallocRecCap);
+            const unsigned long long nl = std::min<unsigned long long>(hcnt[1], kNoallocRecCap);
+            tot_edge += ne;
+            tot_lins += nl;
+            for (unsigned long long r0 = 0; r0 < ne && rp.sppse > 0; r0 += per_chunk) {
+                const long long cnt = (long long)std::min<unsigned long long>(per_chunk, ne - r0);
+                k_edge<N><<<blocks(cnt * rp.sppse), kBlock, 0, st>>>(sc, rp, qe, (long long)r0, cnt, qli, nullptr);
+                if ((rc = launched())) return rc;
+                if ((rc = drain_li())) return rc;
+            }
+            if (nl) {
+                k_lins<N><<<blocks(nl), kBlock, 0, st>>>(sc, rp, ql, nl, acc1, nullptr);
+                if ((rc = launched())) return rc;
+            }
+        }
+    }
+    uint64_t prim_samples = 0;
+    if (o->sppe > 0 && sc.num_pedges > 0) {
+        const long long nblock = (long long)std::ceil(sc.pedge_sum * o->sppe / 128.0);
+        const long long ns = nblock * 128;
+        prim_samples = (uint64_t)ns;
+        rp.prim_weight = sc.pedge_sum / (double)ns;
+        const long long chunk = (long long)(kNoallocLiCap / 2);
+        for (long long k0 = 0; k0 < ns; k0 += chunk) {
+            rp.prim_begin = k0;
+            rp.prim_count = std::min(chunk, ns - k0);
+            k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, nullptr);
+            if ((rc = launched())) return rc;
+            if ((rc = drain_li())) return rc;
+        }
+    }
+    float *dst = out_on_device ? out : stage;
+    k_finalize<N><<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(rp, acc1, acc2, dst);
+    if ((rc = launched())) return rc;
+    if (!out_on_device) DT_CK(cudaMemcpyAsync(out, stage, out_n * 4, cudaMemcpyDeviceToHost, st));
+    unsigned int herr = 0;
+    DT_CK(cudaMemcpyAsync(&herr, err, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    DT_CK(cudaStreamSynchronize(st));
+    dtrt_render_stats &ls = s->last;
+    std::memset(&ls, 0, sizeof(ls));
+    ls.camera_paths = (uint64_t)total;
+    ls.edge_records = tot_edge;
+    ls.lins_records = tot_lins;
+    ls.li_tasks = tot_li;
+    ls.primary_edge_samples = prim_samples;
+    ls.batches = batches;
+    ls.kernel_launches = launches;
+    ls.edge_samples = tot_edge * (uint64_t)rp.sppse;
+    ls.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
+    if (herr & ERR_QUEUE) {
+        set_last_error("work queue overflow");
+        return DTRT_ERR_OVERFLOW;
+    }
+    if (herr & ERR_STACK) {
+        set_last_error("BVH traversal stack overflow");
+        return DTRT_ERR_INVALID;
+    }
+    if (herr & ERR_TRACK_CAP) {
+        set_last_error("a delta/ratio tracking loop hit its iteration cap");
+        return DTRT_ERR_STEP_CAP;
+    }
+    return DTRT_OK;
+}
+
+}  // namespace dt

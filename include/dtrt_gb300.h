@@ -229,6 +229,27 @@ int dtrt_scene_destroy(dtrt_scene *scene);
 int dtrt_render_fwd(dtrt_scene *scene, const dtrt_render_options *opts, float *out,
                     int out_on_device, void *stream);
 
+/* Forward-mode render that allocates no device memory. No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc during a render: code running under a memory
+ * budget fixed at start-up, an embedding runtime that owns all device allocations, or a
+ * host thread that must not take the allocator's locks. Every work buffer this render
+ * needs (FP64 accumulators, task queues, counters, the staging copy of a host `out`)
+ * lives in one file-scope device array of DTRT_NOALLOC_SCRATCH_BYTES (6 MiB), which every
+ * GPU that loads the library keeps until the process exits.
+ *
+ * Limits, rejected with DTRT_ERR_INVALID and a message: at most DTRT_NOALLOC_MAX_PIXELS
+ * output pixels (e.g. 64x64), max_bounces <= 31, sppse <= 8192. Results equal
+ * dtrt_render_fwd's for the same seed up to the order of floating-point atomic adds.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress),
+ * so make that first call before any stream capture. All calls share the one array:
+ * calls whose work overlaps on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller. The call blocks until `out` is written. */
+#define DTRT_NOALLOC_MAX_PIXELS 4096
+#define DTRT_NOALLOC_SCRATCH_BYTES (6u << 20)
+int dtrt_render_fwd_noalloc(dtrt_scene *scene, const dtrt_render_options *opts, float *out,
+                            int out_on_device, void *stream);
+
 /* Enable (1) or disable (0) device work counters for later renders of a scene. */
 int dtrt_scene_enable_counters(dtrt_scene *scene, int enable);
 

@@ -134,6 +134,8 @@ class RenderStats(ctypes.Structure):
 
 
 # Every C-ABI symbol declared in include/dtrt_gb300.h, with its ctypes signature.
+EST_SCATTER_SEGMENT_FROM_ORIGIN = 1
+
 _SIGNATURES = {
     "dtrt_abi_version": (ctypes.c_int, []),
     "dtrt_device_count": (ctypes.c_int, []),
@@ -150,6 +152,14 @@ _SIGNATURES = {
     "dtrt_scene_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderStats)]),
     "dtrt_scene_set_queue_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dtrt_scene_set_tracking_cap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dtrt_scene_set_estimator_flags": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint]),
+    "dtrt_scene_gradient_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                                 ctypes.POINTER(ctypes.c_int64)]),
+    "dtrt_scene_set_density": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p]),
+    "dtrt_scene_set_density_derivatives": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p]),
+    "dtrt_render_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_void_p]),
     "dtrt_trace_closest": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int, c_int_p, c_float_p]),
     "dtrt_vol_read": (ctypes.c_int, [ctypes.c_char_p, c_int_p, c_int_p, c_float_p, c_float_p, c_float_p]),
 }

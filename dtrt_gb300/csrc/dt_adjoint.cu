@@ -1,0 +1,154 @@
+// dtrt_gb300 — host orchestration of the reverse-mode density adjoint (k_adjoint).
+//
+// The replay runs with derivative width 1 whatever the scene's nder: the adjoint needs the
+// path values only, and the per-voxel gradient replaces the derivative slots. The scene
+// copy given to the kernel drops every velocity input so the dual slot stays zero and the
+// no-derivative fast paths apply; values and random decisions are those of dtrt_render_fwd.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+#include "dt_adjoint.cuh"
+#include "dt_host.h"
+
+namespace dt {
+
+#define DT_ACK(call)                                                                 \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_));      \
+            return DTRT_ERR_CUDA;                                                    \
+        }                                                                            \
+    } while (0)
+
+int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
+                   int on_device, cudaStream_t st) {
+    using clk = std::chrono::steady_clock;
+    const auto t_start = clk::now();
+    DevScene sc = s->dev;
+    Scratch &sb = s->scratch;
+    const DevCamera &cam = sc.cam;
+    const bool cropped = cam.crop_w > 0 && cam.crop_h > 0;
+    if (o->max_bounces < 0) {
+        set_last_error("max_bounces must be >= 0");
+        return DTRT_ERR_INVALID;
+    }
+    RenderParams rp{};
+    rp.seed = o->seed;
+    rp.spp = o->spp;
+    rp.max_bounces = o->max_bounces;
+    rp.sppse = 0;  // boundary terms carry no density derivative
+    rp.mode = o->mode >= 0 ? o->mode : MODE_ALL;
+    rp.jitter = o->sppe >= 0 ? 1 : 0;
+    rp.ddist = o->ddist_coeff;
+    rp.inv_spp = o->spp > 0 ? 1.0f / (float)o->spp : 0.f;
+    rp.out_w = cropped ? cam.crop_w : cam.width;
+    rp.out_h = cropped ? cam.crop_h : cam.height;
+    rp.crop_x = cropped ? cam.crop_x : 0;
+    rp.crop_y = cropped ? cam.crop_y : 0;
+    rp.npix = rp.out_w * rp.out_h;
+    const size_t npix = (size_t)rp.npix;
+    // values only: no velocity inputs
+    sc.vert_der = nullptr;
+    sc.face_n_der = nullptr;
+    sc.normal_der = nullptr;
+    sc.moving_geometry = 0;
+    std::memset(sc.cam.d_cpos, 0, sizeof(sc.cam.d_cpos));
+    std::memset(sc.cam.d_cframe, 0, sizeof(sc.cam.d_cframe));
+    if (!sb.err) DT_ACK(cudaMalloc(&sb.err, sizeof(unsigned int)));
+    if (!sb.counts) DT_ACK(cudaMalloc(&sb.counts, 32 * sizeof(unsigned long long)));
+    sc.error_flags = sb.err;
+    DT_ACK(cudaMemsetAsync(sb.err, 0, sizeof(unsigned int), st));
+    DT_ACK(cudaMemsetAsync(sb.counts, 0, 32 * sizeof(unsigned long long), st));
+    unsigned long long *ctr = s->counters ? sb.counts + 8 : nullptr;
+    // ---------------------------------------------------------------- inputs and outputs
+    const float *dimg = nullptr;
+    if (d_image) {
+        if (on_device) {
+            dimg = d_image;
+        } else {
+            if (!ensure_buffer((void **)&sb.adj_dimg, &sb.adj_dimg_n, npix * 3 * 4)) return DTRT_ERR_CUDA;
+            DT_ACK(cudaMemcpyAsync(sb.adj_dimg, d_image, npix * 3 * 4, cudaMemcpyHostToDevice, st));
+            dimg = sb.adj_dimg;
+        }
+    }
+    const size_t nvox = (size_t)s->density_voxels;
+    float *grad = nullptr;
+    if (d_density && nvox > 0) {
+        if (on_device) {
+            grad = d_density;
+        } else {
+            if (!ensure_buffer((void **)&sb.adj_grad, &sb.adj_grad_n, nvox * 4)) return DTRT_ERR_CUDA;
+            grad = sb.adj_grad;
+        }
+        DT_ACK(cudaMemsetAsync(grad, 0, nvox * 4, st));
+    }
+    double *img_acc = nullptr;
+    if (image) {
+        if (!ensure_buffer((void **)&sb.adj_img, &sb.adj_img_n, npix * 3 * 8)) return DTRT_ERR_CUDA;
+        img_acc = sb.adj_img;
+        DT_ACK(cudaMemsetAsync(img_acc, 0, npix * 3 * 8, st));
+    }
+    // ---------------------------------------------------------------- replay
+    cudaEvent_t e0, e1;
+    DT_ACK(cudaEventCreate(&e0));
+    DT_ACK(cudaEventCreate(&e1));
+    const long long total = (long long)npix * std::max(0, o->spp);
+    uint64_t launches = 0;
+    float ms_replay = 0.f;
+    DT_ACK(cudaEventRecord(e0, st));
+    const long long B = 1ll << 24;  // paths per launch
+    for (long long b0 = 0; b0 < total; b0 += B) {
+        rp.path_begin = b0;
+        rp.path_count = std::min(B, total - b0);
+        k_adjoint<1><<<(unsigned)((rp.path_count + kBlock - 1) / kBlock), kBlock, 0, st>>>(sc, rp, dimg, grad, img_acc,
+                                                                                         ctr);
+        ++launches;
+        DT_ACK(cudaGetLastError());
+    }
+    DT_ACK(cudaEventRecord(e1, st));
+    if (image) {
+        float *dst = image;
+        if (!on_device) {
+            if (!ensure_buffer((void **)&sb.adj_out, &sb.adj_out_n, npix * 3 * 4)) return DTRT_ERR_CUDA;
+            dst = sb.adj_out;
+        }
+        k_adjoint_image<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(rp.npix, img_acc, dst);
+        ++launches;
+        DT_ACK(cudaGetLastError());
+        if (!on_device) DT_ACK(cudaMemcpyAsync(image, sb.adj_out, npix * 3 * 4, cudaMemcpyDeviceToHost, st));
+    }
+    if (grad && !on_device) DT_ACK(cudaMemcpyAsync(d_density, grad, nvox * 4, cudaMemcpyDeviceToHost, st));
+    unsigned int herr = 0;
+    unsigned long long hc[CT_NUM] = {0};
+    DT_ACK(cudaMemcpyAsync(&herr, sb.err, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    if (ctr) DT_ACK(cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    DT_ACK(cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&ms_replay, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dtrt_render_stats &ls = s->last;
+    std::memset(&ls, 0, sizeof(ls));
+    ls.camera_paths = (uint64_t)total;
+    ls.kernel_launches = launches;
+    ls.batches = (uint64_t)((total + B - 1) / B);
+    ls.counters_enabled = ctr != nullptr;
+    ls.k_rays[0] = ls.rays = hc[0];
+    ls.k_node_visits[0] = ls.node_visits = hc[1];
+    ls.k_tri_tests[0] = ls.tri_tests = hc[2];
+    ls.k_grid_lookups[0] = ls.grid_lookups = hc[3];
+    ls.ms_camera = ms_replay;
+    ls.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
+    if (herr & ERR_STACK) {
+        set_last_error("BVH traversal stack overflow");
+        return DTRT_ERR_INVALID;
+    }
+    if (herr & ERR_TRACK_CAP) {
+        set_last_error("a delta/ratio tracking loop hit its iteration cap");
+        return DTRT_ERR_STEP_CAP;
+    }
+    return DTRT_OK;
+}
+
+}  // namespace dt

@@ -1,0 +1,241 @@
+// dtrt_gb300 — reverse-mode adjoint of the interior term by path replay.
+//
+// Scope: the gradient of <dL/dI, I> with respect to the density voxels of every
+// heterogeneous medium. The reference has no reverse mode; its forward-mode estimator
+// (volpathAD.cpp:145-620) is the thing differentiated, and this kernel computes the exact
+// transpose of that estimator's per-voxel directional derivative, path by path:
+//
+//   Density enters a camera path only through log-derivative factors:
+//     * distance sampling (heterogeneous.cpp:40-75) multiplies the throughput of every
+//       later event by (sigma_t(p) / sigma_t(p).val) * (1, -int dsigma_t): log-derivative
+//       d density(p) / density(p) - integral, or just -integral when no scatter happens;
+//     * the transmittance of a NEE or emitter-hit segment (heterogeneous.cpp:113-118)
+//       multiplies only that event's contribution: log-derivative -integral.
+//   The integral is the 10-sample stratified estimate of intSigT (heterogeneous.cpp:121-141).
+//
+// So d(path)/d(density) = sum over factors of (log-derivative) * (radiance the factor
+// multiplies). Each thread runs its camera path twice from the same RNG seed:
+//   pass A: the path value, i.e. the sum of its event contributions (the image);
+//   pass B: the same path again; before each distance-sampling factor the suffix radiance
+//           (pass-A total minus what pass B has accumulated so far) is known, so every
+//           density lookup feeding that factor scatters dot(dL/dI, suffix)/spp times its
+//           coefficient into the 8 voxels it read. A NEE or emitter-hit event is first
+//           evaluated for its value, then re-run from the saved RNG state with the weight
+//           dot(dL/dI, event)/spp, which replays the identical random decisions.
+// No path state is stored. Boundary terms (edges, Lins, primary edges) depend on moving
+// geometry only and carry no density derivative, so the replay does not spawn them.
+#pragma once
+#include "dt_kernels.cuh"
+
+namespace dt {
+
+// One camera path of k_camera's loop, value-only, with adjoint scattering in pass B.
+// Must consume the RNG exactly like k_camera: every branch below mirrors it.
+template <int N>
+DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, long long g, int pixel, bool pass_b,
+                        float3 total, float3 gpix, AdjCtx &adj, Ctr &c) {
+    const float3 zero = mk(0.f, 0.f, 0.f);
+    const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
+    Rng rng;
+    rng.init(rp.seed, (uint64_t)g);
+    double jx = 0.5, jy = 0.5;
+    if (rp.jitter) {
+        jx = rng.next1d();
+        jy = rng.next1d();
+    }
+    RayAD<N> ray = camera_ray_ad<N>(sc.cam, ix + jx, iy + jy);
+    ItsAD<N> its;
+    int med = sc.cam.med_id;
+    int depth = rp.max_bounces;
+    int mode = rp.mode;
+    float3 P = mk(1.f, 1.f, 1.f), acc = zero;
+    const AdjCtx *hook = pass_b ? &adj : nullptr;
+    bool alive = ray_intersect_ad<N>(sc, stack, ray, false, its, c);
+    for (int level = 0; alive && mode != 0; ++level) {
+        alive = false;
+        const float r1a = rng.next1(), r1b = rng.next1();
+        float r2[4];
+        r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
+        const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
+        DV<N> thr(mk(1.f, 1.f, 1.f));
+        const float3 dir_in = ray.d.val();
+        if (pass_b) adj.w = dot(gpix, total - acc) * rp.inv_spp;  // suffix radiance of this factor
+        if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c, hook)) {
+            // ------------------------------------------------ volumetric vertex
+            if (depth == 0 || thr.is_zero()) break;
+            const DevPhase &ph = sc.phases[sc.media[med].phase_id];
+            const float3 Q = cmul(P, thr.val());
+            DV<N> wo;
+            float pdf_nee;
+            if (mode & MODE_VOLUME_MAIN) {
+                const Rng saved = rng;
+                DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
+                float3 e = zero;
+                if (!v.is_zero()) {
+                    const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+                    if (pv.v > kEps) e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
+                }
+                if (pass_b && !is_zero3(e, 0.f)) {
+                    const Rng after = rng;
+                    rng = saved;
+                    adj.w = dot(gpix, e) * rp.inv_spp;
+                    DV<N> wo2;
+                    float pdf2;
+                    nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                    rng = after;
+                }
+                acc = acc + e;
+            }
+            const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
+            if (pvs.v > kEps) {
+                const float3 thr1 = thr.val() * pvs.v;
+                ray.d = wo;
+                ItsAD<N> its1;
+                const Rng saved = rng;
+                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
+                                                   nullptr, c);
+                float3 e = zero;
+                if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+                if (pass_b && !is_zero3(e, 0.f)) {
+                    const Rng after = rng;
+                    rng = saved;
+                    adj.w = dot(gpix, e) * rp.inv_spp;
+                    ItsAD<N> its2;
+                    float pdf2;
+                    look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr, c,
+                                           hook);
+                    rng = after;
+                }
+                acc = acc + e;
+                its = its1;
+                P = cmul(P, thr1);
+                depth -= 1;
+                mode &= ~MODE_EMISSION;
+                alive = true;
+            }
+            continue;
+        }
+        // ---------------------------------------------------- interface vertex
+        if (!its.valid() || thr.is_zero()) break;
+        const DevShape &sh = sc.shapes[its.shape];
+        if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) break;
+        const float3 Q = cmul(P, thr.val());
+        if (sh.light_id >= 0 && (mode & MODE_EMISSION)) acc = acc + cmul(Q, le_ad<N>(sc, its, -ray.d).val());
+        if (depth == 0) break;
+        const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
+        const bool is_null = b.type == BSDF_NULL;
+        const FrameAD<N> fr = its.frame();
+        const Its its0 = its.plain();
+        DV<N> wo;
+        float pdf_nee;
+        if (!is_null && (mode & MODE_SURFACE_MAIN)) {
+            const Rng saved = rng;
+            DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+            float3 e = zero;
+            if (!v.is_zero()) {
+                const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
+                const float bp = bsdf_pdf(b, its0.wi, wo.val());
+                e = cmul(cmul(Q, v.val()), bv.val()) * mis_weight(pdf_nee, bp);
+            }
+            if (pass_b && !is_zero3(e, 0.f)) {
+                const Rng after = rng;
+                rng = saved;
+                adj.w = dot(gpix, e) * rp.inv_spp;
+                DV<N> wo2;
+                float pdf2;
+                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                rng = after;
+            }
+            acc = acc + e;
+        }
+        float bpdf, beta;
+        const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
+        if (!bw.is_zero()) {
+            wo = fr.to_world(wo);
+            if (!is_null) wo = zero_grad(wo);
+            ray.o = its.p;
+            ray.d = wo;
+            const int med1 = is_transition(sh) ? target_medium(sc, its.shape, its.ng, wo.val()) : med;
+            float3 thr1 = thr.val();
+            ItsAD<N> its1;
+            if (is_null) {
+                ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
+            } else {
+                const Rng saved = rng;
+                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee, nullptr,
+                                                   nullptr, c);
+                thr1 = cmul(thr1, bw.val());
+                float3 e = zero;
+                if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
+                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(bpdf, pdf_nee);
+                if (pass_b && !is_zero3(e, 0.f)) {
+                    const Rng after = rng;
+                    rng = saved;
+                    adj.w = dot(gpix, e) * rp.inv_spp;
+                    ItsAD<N> its2;
+                    float pdf2;
+                    look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its2, pdf2, nullptr, nullptr, c,
+                                           hook);
+                    rng = after;
+                }
+                acc = acc + e;
+                mode &= ~MODE_EMISSION;
+            }
+            its = its1;
+            P = cmul(P, thr1);
+            med = med1;
+            depth -= 1;
+            alive = true;
+        }
+    }
+    return acc;
+}
+
+// One thread per camera path: pass A (value), then pass B (scatter) when the path and its
+// pixel's dL/dI are non-zero. img_acc (optional) receives the image, FP64 [npix][3].
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp, const float *dimg, float *grad,
+                                                    double *img_acc, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < rp.path_count;
+    const long long g = rp.path_begin + (active ? gi : 0);
+    const int pixel = (int)(g / rp.spp);
+    Ctr c;
+    AdjCtx adj{grad, 0.f};
+    float3 total = mk(0.f, 0.f, 0.f);
+    if (active) {
+        total = replay_path<N>(sc, rp, stack, g, pixel, false, total, total, adj, c);
+        if (grad != nullptr && dimg != nullptr && !is_zero3(total, 0.f)) {
+            const float3 gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1),
+                                 __ldg(dimg + 3 * (size_t)pixel + 2));
+            if (!is_zero3(gp, 0.f)) replay_path<N>(sc, rp, stack, g, pixel, true, total, gp, adj, c);
+        }
+    }
+    if (img_acc != nullptr) {
+        const unsigned full = 0xffffffffu;
+        const int p0 = __shfl_sync(full, pixel, 0);
+        const bool uniform = __all_sync(full, active && pixel == p0);
+        float v[3] = {total.x * rp.inv_spp, total.y * rp.inv_spp, total.z * rp.inv_spp};
+        if (uniform)
+            for (int k = 0; k < 3; ++k)
+                for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(full, v[k], off);
+        if (active && (!uniform || (threadIdx.x & 31) == 0))
+            for (int k = 0; k < 3; ++k)
+                if (v[k] != 0.f) atomicAdd(img_acc + (size_t)pixel * 3 + k, (double)v[k]);
+    }
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// Image write rule of integratorAD.cpp:59-87 (a pixel is written only if non-negative).
+__global__ void k_adjoint_image(int npix, const double *acc, float *out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const double *a = acc + (size_t)p * 3;
+    const bool nonneg = a[0] >= 0.0 && a[1] >= 0.0 && a[2] >= 0.0;
+    for (int c = 0; c < 3; ++c) out[(size_t)p * 3 + c] = nonneg ? (float)a[c] : 0.f;
+}
+
+}  // namespace dt

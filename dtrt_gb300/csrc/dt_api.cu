@@ -523,6 +523,7 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
         const dtrt_medium_desc &md = d->media[mi];
         DevMedium &o = media[mi];
         std::memset(&o, 0, sizeof(o));
+        o.grad_off = -1;
         if (md.phase_id < 0 || md.phase_id >= d->num_phases) return fail("medium phase_id out of range");
         o.type = md.type;
         o.phase_id = md.phase_id;
@@ -553,10 +554,13 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
                 for (int a = 0; a < 3; ++a) {
                     if (md.trans_velocities) o.density.trans_vel[j][a] = md.trans_velocities[3 * j + a];
                     if (md.rot_velocities) o.density.rot_vel[j][a] = md.rot_velocities[3 * j + a];
+                    if (o.density.trans_vel[j][a] != 0.f || o.density.rot_vel[j][a] != 0.f) o.density.moving = 1;
                 }
             }
             if (!(o.scale > 0.f) || !(o.density.max_value > 0.f)) return fail("heterogeneous medium with zero majorant");
             o.max_inv_density = (float)(1.0 / ((double)o.scale * o.density.max_value));
+            o.grad_off = s->density_voxels;
+            s->density_voxels += (long long)o.density.res[0] * o.density.res[1] * o.density.res[2];
         } else {
             return fail("unknown medium type");
         }
@@ -709,6 +713,8 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
     ds.num_phases = d->num_phases;
     ds.num_emitters = d->num_emitters;
     ds.num_media = d->num_media;
+    s->media_host = media;
+    s->dgrid_bufs.assign(d->num_media, nullptr);
     s->num_shapes = d->num_shapes;
     for (int si = 0; si < d->num_shapes; ++si)
         s->shape_skip[si] = (bsdfs[shapes[si].bsdf_id].type == BSDF_NULL && shapes[si].light_id < 0) ? 1 : 0;
@@ -751,11 +757,35 @@ int set_edge_weights(dtrt_scene *s, const float *w) {
 void free_scene(dtrt_scene *s) {
     for (void *p : s->allocs) cudaFree(p);
     s->allocs.clear();
+    for (void *p : s->dgrid_bufs)
+        if (p) cudaFree(p);
+    s->dgrid_bufs.clear();
     Scratch &b = s->scratch;
-    void *ptrs[] = {b.acc1, b.acc2, b.out, b.qe, b.ql, b.qli, b.counts, b.err};
+    void *ptrs[] = {b.acc1, b.acc2, b.out, b.qe, b.ql, b.qli, b.counts, b.err, b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     b = Scratch();
+}
+
+// re-upload the host copy of the media array after a parameter change
+int upload_media(dtrt_scene *s) {
+    if (s->media_host.empty()) return DTRT_OK;
+    cudaError_t e = cudaMemcpy((void *)s->dev.media, s->media_host.data(), s->media_host.size() * sizeof(DevMedium),
+                               cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("media upload: ") + cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
+    }
+    return DTRT_OK;
+}
+
+int check_grid_medium(const dtrt_scene *s, int medium_id) {
+    if (!s || medium_id < 0 || medium_id >= (int)s->media_host.size() ||
+        s->media_host[medium_id].type != MEDIUM_HETEROGENEOUS) {
+        set_last_error("medium_id does not name a heterogeneous medium");
+        return DTRT_ERR_INVALID;
+    }
+    return DTRT_OK;
 }
 
 }  // namespace
@@ -863,6 +893,105 @@ int dtrt_scene_set_tracking_cap(dtrt_scene *scene, int max_steps) {
     if (!scene || max_steps < 0) return DTRT_ERR_INVALID;
     scene->dev.tracking_cap = max_steps;
     return DTRT_OK;
+}
+
+int dtrt_scene_set_estimator_flags(dtrt_scene *scene, unsigned flags) {
+    if (!scene || (flags & ~(unsigned)DTRT_EST_SCATTER_SEGMENT_FROM_ORIGIN)) {
+        dt::set_last_error("unknown estimator flag");
+        return DTRT_ERR_INVALID;
+    }
+    scene->dev.est_flags = flags;
+    return DTRT_OK;
+}
+
+int dtrt_scene_gradient_sizes(const dtrt_scene *scene, int64_t *density_voxels, int64_t *vertices) {
+    if (!scene) {
+        dt::set_last_error("null argument");
+        return DTRT_ERR_INVALID;
+    }
+    if (density_voxels) *density_voxels = scene->density_voxels;
+    if (vertices) *vertices = scene->dev.num_verts;
+    return DTRT_OK;
+}
+
+int dtrt_scene_set_density(dtrt_scene *scene, int medium_id, const float *density) {
+    int st = dt::check_grid_medium(scene, medium_id);
+    if (st) return st;
+    if (!density) {
+        dt::set_last_error("null density");
+        return DTRT_ERR_INVALID;
+    }
+    dt::DevMedium &m = scene->media_host[medium_id];
+    const size_t n = (size_t)m.density.res[0] * m.density.res[1] * m.density.res[2];
+    std::vector<float> v(density, density + n);
+    float maxv = 0.f;
+    for (float &x : v) {  // gridvolume.h:128-131
+        x = std::max(x, 0.0f);
+        maxv = std::max(maxv, x);
+    }
+    if (!(maxv > 0.f)) {
+        dt::set_last_error("heterogeneous medium with zero majorant");
+        return DTRT_ERR_INVALID;
+    }
+    cudaError_t e = cudaMemcpy((void *)m.density.data, v.data(), n * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        dt::set_last_error(std::string("density upload: ") + cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
+    }
+    m.density.max_value = maxv;
+    m.max_inv_density = (float)(1.0 / ((double)m.scale * maxv));
+    return dt::upload_media(scene);
+}
+
+int dtrt_scene_set_density_derivatives(dtrt_scene *scene, int medium_id, const float *grids) {
+    int st = dt::check_grid_medium(scene, medium_id);
+    if (st) return st;
+    dt::DevMedium &m = scene->media_host[medium_id];
+    void *&buf = scene->dgrid_bufs[medium_id];
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    m.density.dgrid = nullptr;
+    m.density.dgrid_n = 0;
+    if (grids) {
+        const int N = scene->nder;
+        const size_t n = (size_t)m.density.res[0] * m.density.res[1] * m.density.res[2];
+        std::vector<float> il(n * N);  // [nder][voxel] -> [voxel][nder]
+        for (int j = 0; j < N; ++j)
+            for (size_t v = 0; v < n; ++v) il[v * N + j] = grids[(size_t)j * n + v];
+        cudaError_t e = cudaMalloc(&buf, il.size() * 4);
+        if (e == cudaSuccess) e = cudaMemcpy(buf, il.data(), il.size() * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            if (buf) cudaFree(buf);
+            buf = nullptr;
+            dt::set_last_error(std::string("density derivative upload: ") + cudaGetErrorString(e));
+            dt::upload_media(scene);
+            return DTRT_ERR_CUDA;
+        }
+        m.density.dgrid = (const float *)buf;
+        m.density.dgrid_n = N;
+    }
+    return dt::upload_media(scene);
+}
+
+int dtrt_render_adjoint(dtrt_scene *scene, const dtrt_render_options *opts, const float *d_image, float *image,
+                        float *d_density, float *d_vertices, int on_device, void *stream) {
+    if (!scene || !opts || (!image && !d_density && !d_vertices)) {
+        dt::set_last_error("null argument");
+        return DTRT_ERR_INVALID;
+    }
+    if (d_vertices) {
+        dt::set_last_error("the vertex-position adjoint is not built; use forward-mode velocities");
+        return DTRT_ERR_UNSUPPORTED;
+    }
+    if (d_density && !d_image) {
+        dt::set_last_error("d_density needs d_image");
+        return DTRT_ERR_INVALID;
+    }
+    if (opts->spp < 0) {
+        dt::set_last_error("spp must be >= 0");
+        return DTRT_ERR_INVALID;
+    }
+    return dt::render_adjoint(scene, opts, d_image, image, d_density, on_device, (cudaStream_t)stream);
 }
 
 }  // extern "C"

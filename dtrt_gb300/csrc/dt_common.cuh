@@ -9,6 +9,14 @@
 
 #define DT_HD __host__ __device__ __forceinline__
 #define DT_D __device__ __forceinline__
+// Large scene queries (BVH traversal, transmittance chains, NEE, BSDF sampling) are called
+// from many places of the path kernels; keeping them out of line keeps each kernel's code
+// inside the instruction cache. DT_INLINE_HEAVY inlines them instead.
+#ifdef DT_INLINE_HEAVY
+#define DT_HEAVY static __device__ __forceinline__
+#else
+#define DT_HEAVY static __device__ __noinline__
+#endif
 
 namespace dt {
 

@@ -57,7 +57,7 @@ constexpr int kStackExit = (int)0x80000000;
 // (the reference bounds them by max_interactions, which can be -1 = unbounded).
 constexpr int kMaxInteractions = 4096;
 
-DT_D int closest_hit(const DevScene &sc, int *stack, float3 o, float3 d, float tmin, float tmax, float &t_hit,
+DT_HEAVY int closest_hit(const DevScene &sc, int *stack, float3 o, float3 d, float tmin, float tmax, float &t_hit,
                      Ctr &c) {
     c.rays++;
     const float3 inv = mk(1.0f / (fabsf(d.x) > 1e-30f ? d.x : copysignf(1e-30f, d.x)),
@@ -213,7 +213,7 @@ struct RayAD {
 
 // utils.cpp:237-254 and shape.cpp:210-252
 template <int N>
-DT_D void shape_intersect_ad(const DevScene &sc, int prim, const RayAD<N> &ray, ItsAD<N> &its) {
+DT_HEAVY void shape_intersect_ad(const DevScene &sc, int prim, const RayAD<N> &ray, ItsAD<N> &its) {
     const int4 tri = __ldg(sc.tris + prim);
     const DV<N> v0 = vertex_ad<N>(sc, tri.x), v1 = vertex_ad<N>(sc, tri.y), v2 = vertex_ad<N>(sc, tri.z);
     const DV<N> e1 = v1 - v0, e2 = v2 - v0, pv = cross(ray.d, e2);
@@ -316,7 +316,7 @@ DT_D float approx_erfinv(float x) {
     }
     return p * x;
 }
-DT_D void sample_visible11(float theta_i, float u, float v, float &sx, float &sy) {  // microfacet.h:178-244
+DT_HEAVY void sample_visible11(float theta_i, float u, float v, float &sx, float &sy) {  // microfacet.h:178-244
     const float SQRT_PI_INV = 0.56418958354775628f;
     if (theta_i < 1e-4f) {
         float r = sqrtf(-logf(1.f - u));
@@ -486,7 +486,7 @@ DT_D float bsdf_pdf(const DevBsdf &b, float3 wi, float3 wo) {
     }
 }
 
-DT_D float3 bsdf_sample(const DevBsdf &b, float3 wi, float r0, float r1, float r2, float3 &wo, float &pdf,
+DT_HEAVY float3 bsdf_sample(const DevBsdf &b, float3 wi, float r0, float r1, float r2, float3 &wo, float &pdf,
                         float &eta) {
     const float3 zero = mk(0.f, 0.f, 0.f);
     switch (b.type) {
@@ -705,6 +705,10 @@ DT_D float grid_lookup(const DevGrid &g, float3 pw, Ctr &c) {  // gridvolume.h:1
 }
 template <int N>
 DT_D Df<N> grid_lookup_ad(const DevGrid &g, const DV<N> &pw, Ctr &c) {  // gridvolume.h:174-201
+    const bool voxel_dirs = g.dgrid != nullptr && g.dgrid_n == N;
+    // A static grid sampled at a point without derivatives has none either: the plain
+    // lookup gives the same dual exactly (all slots zero) at a fraction of the cost.
+    if (!g.moving && !voxel_dirs && pw.der_zero(0.f)) return Df<N>(grid_lookup(g, pw.val(), c));
     c.lookups++;
     const DV<N> p = grid_point_ad<N>(g, pw);
     const int x1 = (int)floorf(p.x.v), y1 = (int)floorf(p.y.v), z1 = (int)floorf(p.z.v);
@@ -712,11 +716,52 @@ DT_D Df<N> grid_lookup_ad(const DevGrid &g, const DV<N> &pw, Ctr &c) {  // gridv
     const Df<N> fx = p.x - (float)x1, fy = p.y - (float)y1, fz = p.z - (float)z1;
     const Df<N> gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
     const int sx = 1, sy = g.res[0], sz = g.res[0] * g.res[1];
-    const float *d = g.data + (size_t)z1 * sz + (size_t)y1 * sy + x1;
+    const size_t base = (size_t)z1 * sz + (size_t)y1 * sy + x1;
+    const float *d = g.data + base;
     const float d000 = __ldg(d), d001 = __ldg(d + sx), d010 = __ldg(d + sy), d011 = __ldg(d + sy + sx);
     const float d100 = __ldg(d + sz), d101 = __ldg(d + sz + sx), d110 = __ldg(d + sz + sy), d111 = __ldg(d + sz + sy + sx);
-    return ((gx * d000 + fx * d001) * gy + (gx * d010 + fx * d011) * fy) * gz +
-           ((gx * d100 + fx * d101) * gy + (gx * d110 + fx * d111) * fy) * fz;
+    Df<N> r = ((gx * d000 + fx * d001) * gy + (gx * d010 + fx * d011) * fy) * gz +
+              ((gx * d100 + fx * d101) * gy + (gx * d110 + fx * d111) * fy) * fz;
+    if (voxel_dirs) {
+        // per-voxel directions: the value derivative d(density)/d(theta_j) at the point
+        const float w[8] = {gx.v * gy.v * gz.v, fx.v * gy.v * gz.v, gx.v * fy.v * gz.v, fx.v * fy.v * gz.v,
+                            gx.v * gy.v * fz.v, fx.v * gy.v * fz.v, gx.v * fy.v * fz.v, fx.v * fy.v * fz.v};
+        const size_t off[8] = {0, (size_t)sx, (size_t)sy, (size_t)(sy + sx), (size_t)sz, (size_t)(sz + sx),
+                               (size_t)(sz + sy), (size_t)(sz + sy + sx)};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float *q = g.dgrid + (base + off[k]) * N;
+#pragma unroll
+            for (int j = 0; j < N; ++j) r.d[j] += w[k] * __ldg(q + j);
+        }
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------ adjoint scatter
+// Reverse-mode hook of the density lookups: the replay kernel sets `w` to the adjoint
+// weight of the log-derivative factor being evaluated; every lookup that feeds that
+// factor adds w * (its coefficient) * (trilinear weight) to the 8 voxels it read.
+struct AdjCtx {
+    float *grad;  // density gradient of all heterogeneous media (DevMedium::grad_off)
+    float w;
+};
+DT_D void grid_scatter(const DevGrid &g, float *grad, float3 pw, float w) {
+    if (w == 0.f) return;
+    const float3 p = grid_point(g, pw);
+    const int x1 = (int)floorf(p.x), y1 = (int)floorf(p.y), z1 = (int)floorf(p.z);
+    if (x1 < 0 || x1 + 1 >= g.res[0] || y1 < 0 || y1 + 1 >= g.res[1] || z1 < 0 || z1 + 1 >= g.res[2]) return;
+    const float fx = p.x - x1, fy = p.y - y1, fz = p.z - z1, gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
+    const int sy = g.res[0], sz = g.res[0] * g.res[1];
+    float *q = grad + (size_t)z1 * sz + (size_t)y1 * sy + x1;
+    atomicAdd(q, w * gx * gy * gz);
+    atomicAdd(q + 1, w * fx * gy * gz);
+    atomicAdd(q + sy, w * gx * fy * gz);
+    atomicAdd(q + sy + 1, w * fx * fy * gz);
+    atomicAdd(q + sz, w * gx * gy * fz);
+    atomicAdd(q + sz + 1, w * fx * gy * fz);
+    atomicAdd(q + sz + sy, w * gx * fy * fz);
+    atomicAdd(q + sz + sy + 1, w * fx * fy * fz);
 }
 DT_D float3 grid_lookup3(const DevGrid &g, float3 pw) {  // gridvolume.h:204-232
     const float3 p = grid_point(g, pw);
@@ -773,7 +818,7 @@ DT_D float3 sig_s(const DevMedium &m, float3 x, Ctr &c) {  // homogeneous.h:57, 
 }
 
 // homogeneous.cpp:6-24 / heterogeneous.cpp:9-37; moves `o` to the scatter point
-DT_D bool sample_distance(const DevScene &sc, const DevMedium &m, float3 &o, float3 d, float tmax, float r0, float r1,
+DT_HEAVY bool sample_distance(const DevScene &sc, const DevMedium &m, float3 &o, float3 d, float tmax, float r0, float r1,
                           Rng &rng, float3 &thr, Ctr &c) {
     if (m.type == MEDIUM_HOMOGENEOUS) {
         if (m.sampling_weight > kEps) {
@@ -813,19 +858,24 @@ DT_D bool sample_distance(const DevScene &sc, const DevMedium &m, float3 &o, flo
 }
 
 // heterogeneous.cpp:121-141: -d/dtheta of the optical depth over [tmin, tmax]
+// With `adj`, each sample also scatters adj->w * (-scale * len / 10) into the gradient:
+// the factor exp(-optical depth) has log-derivative -(this integral).
 template <int N>
-DT_D void int_sig_t(const DevScene &sc, const DevMedium &m, const RayAD<N> &ray, const Df<N> &tmin, const Df<N> &tmax,
-                    Rng &rng, float out[N], Ctr &c) {
+DT_HEAVY void int_sig_t(const DevScene &sc, const DevMedium &m, const RayAD<N> &ray, const Df<N> &tmin, const Df<N> &tmax,
+                    Rng &rng, float out[N], Ctr &c, const AdjCtx *adj = nullptr) {
     const Df<N> scale = load_dual<N>(m.scale, m.d_scale);
 #pragma unroll
     for (int j = 0; j < N; ++j) out[j] = 0.f;
     const float len = tmax.v - tmin.v;
+    const bool scatter = adj != nullptr && m.grad_off >= 0;
     for (int i = 0; i < 10; ++i) {
         const float r = ((float)i + rng.next1()) * 0.1f;
         const Df<N> tt = tmin + len * r;
-        const Df<N> s = scale * grid_lookup_ad<N>(m.density, ray.o + ray.d * tt, c);
+        const DV<N> pt = ray.o + ray.d * tt;
+        const Df<N> s = scale * grid_lookup_ad<N>(m.density, pt, c);
 #pragma unroll
         for (int j = 0; j < N; ++j) out[j] += s.d[j];
+        if (scatter) grid_scatter(m.density, adj->grad + m.grad_off, pt.val(), -adj->w * m.scale * len * 0.1f);
     }
 #pragma unroll
     for (int j = 0; j < N; ++j) out[j] *= len * 0.1f;
@@ -843,9 +893,10 @@ DT_D void int_sig_t(const DevScene &sc, const DevMedium &m, const RayAD<N> &ray,
 }
 
 // homogeneous.cpp:27-49 / heterogeneous.cpp:40-75; moves ray.o to the scatter point
+// With `adj`, the factor applied to `thr` scatters adj->w times its log-derivative.
 template <int N>
-DT_D bool sample_distance_ad(const DevScene &sc, const DevMedium &m, RayAD<N> &ray, const Df<N> &tmax, float r0,
-                             float r1, Rng &rng, DV<N> &thr, Ctr &c) {
+DT_HEAVY bool sample_distance_ad(const DevScene &sc, const DevMedium &m, RayAD<N> &ray, const Df<N> &tmax, float r0,
+                             float r1, Rng &rng, DV<N> &thr, Ctr &c, const AdjCtx *adj = nullptr) {
     if (m.type == MEDIUM_HOMOGENEOUS) {
         const Df<N> sig = load_dual<N>(m.sigma_t, m.d_sigma_t);
         if (m.sampling_weight > kEps) {
@@ -886,11 +937,16 @@ DT_D bool sample_distance_ad(const DevScene &sc, const DevMedium &m, RayAD<N> &r
         if (rng.next1() * m.density.max_value < dens.v) {
             // The reference aliases p_scatter with ray.org (volpathAD.cpp:164), so the
             // line integral below runs from the scatter point forward over [0, t].
+            // EST_SCATTER_FROM_ORIGIN integrates the segment actually travelled instead.
+            const RayAD<N> ray0 = ray;
             ray.o = p;
             const DV<N> alb = m.albedo_vol.valid ? grid_lookup3_ad<N>(m.albedo_vol, p) : load_dual3<N>(m.albedo, m.d_albedo);
             const Df<N> sig = load_dual<N>(m.scale, m.d_scale) * dens;
+            if (adj != nullptr && m.grad_off >= 0)  // d log(sigma_t(p)) = d density / density
+                grid_scatter(m.density, adj->grad + m.grad_off, p.val(), adj->w / dens.v);
             float ist[N];
-            int_sig_t<N>(sc, m, ray, Df<N>(0.f), Df<N>(t), rng, ist, c);
+            int_sig_t<N>(sc, m, (sc.est_flags & EST_SCATTER_FROM_ORIGIN) ? ray0 : ray, Df<N>(0.f), Df<N>(t), rng, ist,
+                         c, adj);
             Df<N> tmp(1.f);
 #pragma unroll
             for (int j = 0; j < N; ++j) tmp.d[j] = -ist[j];
@@ -899,7 +955,7 @@ DT_D bool sample_distance_ad(const DevScene &sc, const DevMedium &m, RayAD<N> &r
         }
     }
     float ist[N];
-    int_sig_t<N>(sc, m, ray, Df<N>(0.f), tmax, rng, ist, c);
+    int_sig_t<N>(sc, m, ray, Df<N>(0.f), tmax, rng, ist, c, adj);
     Df<N> tmp(1.f);
 #pragma unroll
     for (int j = 0; j < N; ++j) tmp.d[j] = -ist[j];
@@ -908,7 +964,7 @@ DT_D bool sample_distance_ad(const DevScene &sc, const DevMedium &m, RayAD<N> &r
 }
 
 // homogeneous.cpp:52-55 / heterogeneous.cpp:78-91 (residual ratio tracking)
-DT_D float medium_transmittance(const DevScene &sc, const DevMedium &m, float3 o, float3 d, float tmin, float tmax,
+DT_HEAVY float medium_transmittance(const DevScene &sc, const DevMedium &m, float3 o, float3 d, float tmin, float tmax,
                                 Rng &rng, Ctr &c) {
     if (m.type == MEDIUM_HOMOGENEOUS) return expf((tmin - tmax) * m.sigma_t);
     float ret = 1.f, t = tmin;
@@ -925,12 +981,12 @@ DT_D float medium_transmittance(const DevScene &sc, const DevMedium &m, float3 o
     return ret;
 }
 template <int N>
-DT_D Df<N> medium_transmittance_ad(const DevScene &sc, const DevMedium &m, const RayAD<N> &ray, float tmin,
-                                   const Df<N> &tmax, Rng &rng, Ctr &c) {
+DT_HEAVY Df<N> medium_transmittance_ad(const DevScene &sc, const DevMedium &m, const RayAD<N> &ray, float tmin,
+                                   const Df<N> &tmax, Rng &rng, Ctr &c, const AdjCtx *adj = nullptr) {
     if (m.type == MEDIUM_HOMOGENEOUS) return dexp((tmin - tmax) * load_dual<N>(m.sigma_t, m.d_sigma_t));
     Df<N> ret(medium_transmittance(sc, m, ray.o.val(), ray.d.val(), tmin, tmax.v, rng, c));  // heterogeneous.cpp:113-118
     float ist[N];
-    int_sig_t<N>(sc, m, ray, Df<N>(tmin), tmax, rng, ist, c);
+    int_sig_t<N>(sc, m, ray, Df<N>(tmin), tmax, rng, ist, c, adj);
 #pragma unroll
     for (int j = 0; j < N; ++j) ret.d[j] = -ret.v * ist[j];
     return ret;
@@ -964,7 +1020,7 @@ DT_D bool ray_intersect_ad(const DevScene &sc, int *stack, const RayAD<N> &ray, 
 }
 
 // scene.cpp:177-237
-DT_D float eval_transmittance(const DevScene &sc, int *stack, float3 o, float3 d, bool on_surface, int med,
+DT_HEAVY float eval_transmittance(const DevScene &sc, int *stack, float3 o, float3 d, bool on_surface, int med,
                               float remaining, Rng &rng, int max_inter, Ctr &c) {
     float tmin = on_surface ? kShadowEps : 0.f;
     float tfar = (1.f - kShadowEps) * remaining;
@@ -995,7 +1051,7 @@ DT_D float eval_transmittance(const DevScene &sc, int *stack, float3 o, float3 d
 }
 
 // scene.cpp:617-701
-DT_D float3 look_for_emitter(const DevScene &sc, int *stack, float3 o, float3 d, bool on_surface, Rng &rng, int med,
+DT_HEAVY float3 look_for_emitter(const DevScene &sc, int *stack, float3 o, float3 d, bool on_surface, Rng &rng, int med,
                              int max_inter, Its &its, float &pdf_nee, Ctr &c) {
     float tmin = on_surface ? kShadowEps : 0.f, th;
     const float3 scatter = o;
@@ -1032,8 +1088,9 @@ DT_D float3 look_for_emitter(const DevScene &sc, int *stack, float3 o, float3 d,
 
 // scene.cpp:703-793
 template <int N>
-DT_D DV<N> look_for_emitter_ad(const DevScene &sc, int *stack, RayAD<N> ray, bool on_surface, Rng &rng, int med,
-                               int max_inter, ItsAD<N> &its, float &pdf_nee, int *far_shape, float *far_t, Ctr &c) {
+DT_HEAVY DV<N> look_for_emitter_ad(const DevScene &sc, int *stack, RayAD<N> ray, bool on_surface, Rng &rng, int med,
+                               int max_inter, ItsAD<N> &its, float &pdf_nee, int *far_shape, float *far_t, Ctr &c,
+                               const AdjCtx *adj = nullptr) {
     float tmin = on_surface ? kShadowEps : 0.f, th;
     const float3 scatter = ray.o.val();
     int prim = closest_hit(sc, stack, ray.o.val(), ray.d.val(), tmin, INFINITY, th, c);
@@ -1049,7 +1106,7 @@ DT_D DV<N> look_for_emitter_ad(const DevScene &sc, int *stack, RayAD<N> ray, boo
         if (inter > 0) shape_intersect_ad<N>(sc, prim, ray, ni);
         const Df<N> tmax = ni.t;
         dist += ni.t;
-        if (med >= 0) tr *= medium_transmittance_ad<N>(sc, sc.media[med], ray, tmin, tmax, rng, c);
+        if (med >= 0) tr *= medium_transmittance_ad<N>(sc, sc.media[med], ray, tmin, tmax, rng, c, adj);
         const DevShape &s = sc.shapes[ni.shape];
         if (s.light_id >= 0) {
             const float3 dp = ni.p.val() - scatter;
@@ -1072,7 +1129,7 @@ DT_D DV<N> look_for_emitter_ad(const DevScene &sc, int *stack, RayAD<N> ray, boo
 }
 
 // scene.cpp:399-426 (from a point in a medium; wo in world space)
-DT_D float3 nee_point(const DevScene &sc, int *stack, float3 p, const float rnd[4], Rng &rng, int med, int max_inter,
+DT_HEAVY float3 nee_point(const DevScene &sc, int *stack, float3 p, const float rnd[4], Rng &rng, int med, int max_inter,
                       float3 &wo, float &pdf, Ctr &c) {
     float3 lp, ln;
     const int l = sample_light(sc, rnd, lp, ln, pdf);
@@ -1092,7 +1149,7 @@ DT_D float3 nee_point(const DevScene &sc, int *stack, float3 p, const float rnd[
 }
 
 // scene.cpp:456-491 (from a surface; wo in the local shading frame)
-DT_D float3 nee_surface(const DevScene &sc, int *stack, const Its &its, const float rnd[4], Rng &rng, int med,
+DT_HEAVY float3 nee_surface(const DevScene &sc, int *stack, const Its &its, const float rnd[4], Rng &rng, int med,
                         int max_inter, float3 &wo, float &pdf, bool flag, Ctr &c) {
     float3 lp, ln;
     const int l = sample_light(sc, rnd, lp, ln, pdf);
@@ -1120,8 +1177,8 @@ DT_D float3 nee_surface(const DevScene &sc, int *stack, const Its &its, const fl
 
 // scene.cpp:428-454 (AD, from a point; the light sample carries no derivative)
 template <int N>
-DT_D DV<N> nee_point_ad(const DevScene &sc, int *stack, const DV<N> &p, const float rnd[4], Rng &rng, int med,
-                        int max_inter, DV<N> &wo, float &pdf, Ctr &c) {
+DT_HEAVY DV<N> nee_point_ad(const DevScene &sc, int *stack, const DV<N> &p, const float rnd[4], Rng &rng, int med,
+                        int max_inter, DV<N> &wo, float &pdf, Ctr &c, const AdjCtx *adj = nullptr) {
     float3 lp, ln;
     float pdf0;
     const int l = sample_light(sc, rnd, lp, ln, pdf0);
@@ -1134,7 +1191,8 @@ DT_D DV<N> nee_point_ad(const DevScene &sc, int *stack, const DV<N> &p, const fl
         int far_shape = -1;
         float far_t = 0.f;
         RayAD<N> r{p, DV<N>(dir)};
-        DV<N> v = look_for_emitter_ad<N>(sc, stack, r, false, rng, med, max_inter, near_its, pdf, &far_shape, &far_t, c);
+        DV<N> v = look_for_emitter_ad<N>(sc, stack, r, false, rng, med, max_inter, near_its, pdf, &far_shape, &far_t, c,
+                                         adj);
         if (!v.is_zero() && pdf > kEps && far_shape == sc.emitters[l].shape_id && fabsf(far_t - dist) < kShadowEps) {
             wo = DV<N>(dir);
             return v / pdf;
@@ -1145,8 +1203,8 @@ DT_D DV<N> nee_point_ad(const DevScene &sc, int *stack, const DV<N> &p, const fl
 
 // scene.cpp:493-524 (AD, from a surface; wo in the dual shading frame)
 template <int N>
-DT_D DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &its, const FrameAD<N> &fr, const float rnd[4],
-                          Rng &rng, int med, int max_inter, DV<N> &wo, float &pdf, Ctr &c) {
+DT_HEAVY DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &its, const FrameAD<N> &fr, const float rnd[4],
+                          Rng &rng, int med, int max_inter, DV<N> &wo, float &pdf, Ctr &c, const AdjCtx *adj = nullptr) {
     float3 lp, ln;
     float pdf0;
     const int l = sample_light(sc, rnd, lp, ln, pdf0);
@@ -1163,7 +1221,8 @@ DT_D DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &its, c
         int far_shape = -1;
         float far_t = 0.f;
         RayAD<N> r{its.p, DV<N>(dir)};
-        DV<N> v = look_for_emitter_ad<N>(sc, stack, r, true, rng, med, max_inter, near_its, pdf, &far_shape, &far_t, c);
+        DV<N> v = look_for_emitter_ad<N>(sc, stack, r, true, rng, med, max_inter, near_its, pdf, &far_shape, &far_t, c,
+                                         adj);
         if (!v.is_zero() && pdf > kEps && far_shape == sc.emitters[l].shape_id && fabsf(far_t - dist) < kShadowEps) {
             wo = fr.to_local(dir);
             return v / pdf;

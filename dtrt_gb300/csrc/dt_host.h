@@ -20,6 +20,10 @@ struct Scratch {
     size_t qe_bytes = 0, ql_bytes = 0, qli_bytes = 0;
     unsigned long long *counts = nullptr;  // [0] edge recs, [1] lins recs, [2] li tasks, [8..] counters
     unsigned int *err = nullptr;
+    // adjoint render: dL/dI staging, density gradient, FP64 image accumulator, image staging
+    float *adj_dimg = nullptr, *adj_grad = nullptr, *adj_out = nullptr;
+    double *adj_img = nullptr;
+    size_t adj_dimg_n = 0, adj_grad_n = 0, adj_out_n = 0, adj_img_n = 0;
 };
 
 }  // namespace dt
@@ -36,12 +40,17 @@ struct dtrt_scene {
     int num_shapes = 0;
     std::vector<float> shape_edge_len;  // per shape total edge length (for re-weighting)
     std::vector<int> shape_skip;        // null-BSDF shapes without emitter
+    std::vector<dt::DevMedium> media_host;  // host copy of the device media array
+    std::vector<void *> dgrid_bufs;         // per medium: per-voxel derivative directions (owned)
+    long long density_voxels = 0;           // voxels of all heterogeneous media (adjoint gradient length)
 };
 
 namespace dt {
 template <int N>
 int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream);
 bool ensure_buffer(void **ptr, size_t *have, size_t need);
+int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
+                   int on_device, cudaStream_t stream);
 template <int N>
 int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream,
                      unsigned char *scratch, size_t scratch_bytes);

@@ -59,6 +59,11 @@ struct DevGrid {
     float center[3], lo[3], hi[3]; // rotation centre and world AABB
     float max_value;
     float trans_vel[kMaxNder][3], rot_vel[kMaxNder][3];
+    int moving;  // any non-zero velocity slot
+    // per-voxel derivative directions (density grids only): [voxel][dgrid_n]; slot j of a
+    // lookup's derivative gains the trilinear interpolation of direction j. NULL: none.
+    const float *dgrid;
+    int dgrid_n;
 };
 
 struct DevMedium {
@@ -68,6 +73,7 @@ struct DevMedium {
     float sigma_s[3], sampling_weight;
     float scale, d_scale[kMaxNder], max_inv_density;
     DevGrid density, albedo_vol;
+    long long grad_off;  // offset of this medium's voxels in the adjoint density gradient (-1: none)
 };
 
 struct DevShape {
@@ -137,9 +143,13 @@ struct DevScene {
     DevCamera cam;
     int tracking_cap;
     int moving_geometry;           // any vertex velocity present
+    unsigned est_flags;            // estimator variants, EST_* (0: the reference's estimator)
     unsigned int *error_flags;     // device flags: bit0 stack overflow, bit1 tracking cap, bit2 queue overflow
 };
 
 enum { ERR_STACK = 1u, ERR_TRACK_CAP = 2u, ERR_QUEUE = 4u };
+// EST_SCATTER_FROM_ORIGIN: the free-flight derivative integral of a scatter event runs over
+// [ray origin, scatter point] instead of the reference's [scatter point, scatter point + t*d]
+enum { EST_SCATTER_FROM_ORIGIN = 1u };
 
 }  // namespace dt

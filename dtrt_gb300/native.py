@@ -55,6 +55,28 @@ class NativeScene:
     def set_tracking_cap(self, n):
         _abi.check(self.lib.dtrt_scene_set_tracking_cap(self.handle, int(n)))
 
+    def set_estimator_flags(self, flags):
+        _abi.check(self.lib.dtrt_scene_set_estimator_flags(self.handle, int(flags)))
+
+    def gradient_sizes(self):
+        nv, nvert = ctypes.c_int64(), ctypes.c_int64()
+        _abi.check(self.lib.dtrt_scene_gradient_sizes(self.handle, ctypes.byref(nv), ctypes.byref(nvert)))
+        return nv.value, nvert.value
+
+    def set_density(self, medium_id, density):
+        d = np.ascontiguousarray(density, np.float32)
+        _abi.check(self.lib.dtrt_scene_set_density(self.handle, int(medium_id), d.ctypes.data_as(_abi.c_float_p)))
+
+    def set_density_derivatives(self, medium_id, grids):
+        """grids: [nder, rz, ry, rx] per-voxel directions (None removes them)."""
+        if grids is None:
+            _abi.check(self.lib.dtrt_scene_set_density_derivatives(self.handle, int(medium_id), None))
+            return
+        g = np.ascontiguousarray(grids, np.float32)
+        assert g.shape[0] == self.nder
+        _abi.check(self.lib.dtrt_scene_set_density_derivatives(self.handle, int(medium_id),
+                                                               g.ctypes.data_as(_abi.c_float_p)))
+
     def last_stats(self):
         st = _abi.RenderStats()
         _abi.check(self.lib.dtrt_scene_last_stats(self.handle, ctypes.byref(st)))
@@ -80,6 +102,35 @@ class NativeScene:
         _abi.check(self.lib.dtrt_render_fwd(self.handle, ctypes.byref(o), out.ctypes.data_as(ctypes.c_void_p), 0,
                                              ctypes.c_void_p(stream or 0)))
         return out
+
+    def render_adjoint(self, d_image=None, image=True, density_grad=True, stream=None, device=False, **kw):
+        """Reverse-mode density adjoint (dtrt_render_adjoint).
+
+        Host mode (device=False): `d_image` is a float32 [H, W, 3] array; returns
+        (image or None, d_density or None) as new host arrays.
+        Device mode (device=True): `d_image`, `image` and `density_grad` are device
+        pointers (ints, or None/0 to skip) on `stream`; returns None."""
+        o = kw.pop("options", None) or self.options(**kw)
+        vp = ctypes.c_void_p
+        if device:
+            _abi.check(self.lib.dtrt_render_adjoint(self.handle, ctypes.byref(o), vp(d_image or 0),
+                                                     vp(image if isinstance(image, int) else 0),
+                                                     vp(density_grad if isinstance(density_grad, int) else 0), None, 1,
+                                                     vp(stream or 0)))
+            return None
+        h, w = self.spec.out_shape()[1:3]
+        img = np.zeros((h, w, 3), np.float32) if image else None
+        grad = None
+        if density_grad:
+            grad = np.zeros(self.gradient_sizes()[0], np.float32)
+        dimg = None
+        if d_image is not None:
+            dimg = np.ascontiguousarray(d_image, np.float32)
+            assert dimg.shape == (h, w, 3)
+        ptr = lambda a: a.ctypes.data_as(vp) if a is not None else None
+        _abi.check(self.lib.dtrt_render_adjoint(self.handle, ctypes.byref(o), ptr(dimg), ptr(img), ptr(grad), None, 0,
+                                                 vp(stream or 0)))
+        return img, grad
 
     def trace_closest(self, rays):
         rays = np.ascontiguousarray(rays, np.float32)

@@ -265,6 +265,50 @@ int dtrt_scene_set_queue_capacity(dtrt_scene *scene, uint64_t max_tasks);
  * returns DTRT_ERR_STEP_CAP. */
 int dtrt_scene_set_tracking_cap(dtrt_scene *scene, int max_steps);
 
+/* ---------------------------------------------------------------- reverse mode and density
+ * parameters. None of these has a counterpart in the reference: its heterogeneous medium
+ * differentiates the lookup position, the density scale and the albedo only
+ * (src/medium/heterogeneous.h:46-75, include/gridvolume.h:174-201), and it has no reverse
+ * mode; pydtrt re-reads the VOL file to change a grid (pydtrt/scene_manager.py:286-297). */
+
+/* Estimator variants (bit mask, 0 = the reference's estimator).
+ * DTRT_EST_SCATTER_SEGMENT_FROM_ORIGIN: at a delta-tracking scatter event the derivative of
+ * the free-flight optical depth is integrated over the segment travelled, [ray origin,
+ * scatter point]. The reference passes ray.org as the scatter-point output of
+ * sampleDistanceAD (volpathAD.cpp:164), so its intSigT(ray, 0, t) runs over
+ * [scatter point, scatter point + t*d] (heterogeneous.cpp:65); that is the default here too. */
+#define DTRT_EST_SCATTER_SEGMENT_FROM_ORIGIN 1u
+int dtrt_scene_set_estimator_flags(dtrt_scene *scene, unsigned flags);
+
+/* Sizes of the adjoint outputs: voxels of all heterogeneous media (concatenated in medium
+ * order, each [res_z][res_y][res_x]) and scene vertices (shape order). Either may be NULL. */
+int dtrt_scene_gradient_sizes(const dtrt_scene *scene, int64_t *density_voxels, int64_t *vertices);
+
+/* Replace the density grid of heterogeneous medium `medium_id` (same resolution, values
+ * clamped at 0 as on load); the majorant is recomputed. */
+int dtrt_scene_set_density(dtrt_scene *scene, int medium_id, const float *density);
+
+/* Per-voxel directional derivatives of a heterogeneous medium's density for forward mode:
+ * grids is [nder][res_z][res_y][res_x]; derivative slot j of every density lookup in the
+ * medium gains the trilinear interpolation of grids[j] (its directional derivative along
+ * grid j). NULL removes them. */
+int dtrt_scene_set_density_derivatives(dtrt_scene *scene, int medium_id, const float *grids);
+
+/* Reverse-mode adjoint by path replay: the gradient of sum(d_image * I) with respect to
+ * every density voxel, where I is the expected image of dtrt_render_fwd slot 0 for these
+ * options. Each camera path is traced twice from its RNG seed (value, then replay with
+ * scattering); nothing is stored per path. The estimate is the exact transpose of the
+ * forward-mode per-voxel derivative of the same paths: projecting d_density on a direction
+ * grid equals sum(d_image * derivative image) of dtrt_render_fwd with that direction set by
+ * dtrt_scene_set_density_derivatives, for the same seed, up to rounding.
+ *   d_image    [H][W][3] dL/dI (crop size when cropped); required with d_density
+ *   image      NULL or out [H][W][3]: the image of the same paths
+ *   d_density  NULL or out [density_voxels] (dtrt_scene_gradient_sizes), overwritten
+ *   d_vertices must be NULL (vertex-position adjoint: DTRT_ERR_UNSUPPORTED)
+ * Pointers are host memory when on_device == 0, else device memory on `stream`. */
+int dtrt_render_adjoint(dtrt_scene *scene, const dtrt_render_options *opts, const float *d_image, float *image,
+                        float *d_density, float *d_vertices, int on_device, void *stream);
+
 /* Closest-hit queries against the scene BVH (device kernel), for tests of the
  * traversal. rays: [n][8] = org.xyz, tmin, dir.xyz, tmax (host arrays).
  * hits: [n][2] int = (global triangle id or -1, shape id); t: [n] float. */

@@ -30,6 +30,13 @@ extern "C" {
  * Returns 0 on success; non-zero with oracle_last_error() otherwise. */
 int oracle_render(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads);
 
+/* oracle_render with the extensions of the CUDA library that have no reference
+ * counterpart: estimator flags (dtrt_scene_set_estimator_flags) and per-voxel density
+ * directions per medium (dtrt_scene_set_density_derivatives; density_dirs[m] NULL or
+ * [nder][res_z][res_y][res_x]; density_dirs itself may be NULL). */
+int oracle_render_ext(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads,
+                      unsigned est_flags, const float *const *density_dirs);
+
 /* Render only the primary-edge pass (integratorAD.cpp:100-165) with a caller-chosen
  * sample count, into out[nder][H][W][3] (added to). */
 int oracle_render_primary_edges(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out,

@@ -33,6 +33,7 @@ def lib():
         ip = ctypes.POINTER(ctypes.c_int)
         L.oracle_render.argtypes = [SD, RO, fp, ctypes.c_int]
         L.oracle_render_primary_edges.argtypes = [SD, RO, fp, ctypes.c_int]
+        L.oracle_render_ext.argtypes = [SD, RO, fp, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(fp)]
         L.oracle_pcg32.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
         L.oracle_pcg32.restype = None
         L.oracle_next1d.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, dp]
@@ -62,6 +63,28 @@ def render(spec, seed=0, spp=4, max_bounces=5, sppe=0, sppse=10, mode=-1, ddist=
                             nthreads)
     if r:
         raise RuntimeError("oracle_render: " + lib().oracle_last_error().decode())
+    return out
+
+
+def render_ext(spec, seed=0, spp=4, max_bounces=5, sppe=0, sppse=10, mode=-1, ddist=0.0, nthreads=0, est_flags=0,
+               density_dirs=None):
+    """render() with estimator flags and per-medium per-voxel density directions
+    (density_dirs: {medium_id: float32[nder, rz, ry, rx]})."""
+    desc, keep = spec.to_desc()
+    out = np.zeros(spec.out_shape(), np.float32)
+    o = _opts(seed, spp, max_bounces, sppe, sppse, mode, ddist)
+    fp = ctypes.POINTER(ctypes.c_float)
+    nm = len(spec.media)
+    arr = (fp * max(nm, 1))()
+    held = []
+    for mi, g in (density_dirs or {}).items():
+        g = np.ascontiguousarray(g, np.float32)
+        held.append(g)
+        arr[mi] = g.ctypes.data_as(fp)
+    r = lib().oracle_render_ext(ctypes.byref(desc), ctypes.byref(o), out.ctypes.data_as(fp), nthreads, est_flags,
+                                arr if density_dirs else None)
+    if r:
+        raise RuntimeError("oracle_render_ext: " + lib().oracle_last_error().decode())
     return out
 
 

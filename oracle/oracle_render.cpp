@@ -958,13 +958,26 @@ thread_local std::string g_err;
 
 template <int N>
 int render_impl(const dtrt_scene_desc &d, const dtrt_render_options &o, float *out, int nthreads, bool pass1,
-                bool pass2) {
+                bool pass2, unsigned est_flags = 0, const float *const *density_dirs = nullptr) {
     using namespace orc;
     auto sc = std::make_unique<Scene<N>>();
     std::string err = sc->build(d);
     if (!err.empty()) {
         g_err = err;
         return 1;
+    }
+    sc->est_flags = est_flags;
+    for (int mi = 0; density_dirs && mi < d.num_media; ++mi) {
+        Grid<N> &g = sc->media[mi].density;
+        if (!density_dirs[mi]) continue;
+        if (sc->media[mi].type != DTRT_MEDIUM_HETEROGENEOUS) {
+            g_err = "density directions given for a homogeneous medium";
+            return 1;
+        }
+        const size_t n = (size_t)g.res[0] * g.res[1] * g.res[2];
+        g.dgrid.assign(n * N, 0.f);  // [nder][voxel] -> [voxel][nder]
+        for (int j = 0; j < N; ++j)
+            for (size_t v = 0; v < n; ++v) g.dgrid[v * N + j] = density_dirs[mi][(size_t)j * n + v];
     }
     Integrator<N> in(*sc, o.sppse, o.ddist_coeff);
     const Camera<N> &cam = sc->cam;
@@ -1081,6 +1094,14 @@ extern "C" {
 int oracle_render(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads) {
     if (!desc || !opts || !out) { g_err = "null argument"; return 1; }
     return dispatch(desc->nder, [&](auto n) { return render_impl<decltype(n)::value>(*desc, *opts, out, nthreads, true, true); });
+}
+
+int oracle_render_ext(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads,
+                      unsigned est_flags, const float *const *density_dirs) {
+    if (!desc || !opts || !out) { g_err = "null argument"; return 1; }
+    return dispatch(desc->nder, [&](auto n) {
+        return render_impl<decltype(n)::value>(*desc, *opts, out, nthreads, true, true, est_flags, density_dirs);
+    });
 }
 
 int oracle_render_primary_edges(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads) {

@@ -236,8 +236,17 @@ Dual<N> Grid<N>::lookup_ad(const DV3<N> &pw) const {  // gridvolume.h:174-201
     Dual<N> fx = p.x - (double)x1, fy = p.y - (double)y1, fz = p.z - (double)z1;
     Dual<N> gx = 1.0 - fx, gy = 1.0 - fy, gz = 1.0 - fz;
     auto D = [&](int z, int y, int x) { return (double)data[((size_t)z * res[1] + y) * res[0] + x]; };
-    return ((D(z1, y1, x1) * gx + D(z1, y1, x2) * fx) * gy + (D(z1, y2, x1) * gx + D(z1, y2, x2) * fx) * fy) * gz +
-           ((D(z2, y1, x1) * gx + D(z2, y1, x2) * fx) * gy + (D(z2, y2, x1) * gx + D(z2, y2, x2) * fx) * fy) * fz;
+    Dual<N> r = ((D(z1, y1, x1) * gx + D(z1, y1, x2) * fx) * gy + (D(z1, y2, x1) * gx + D(z1, y2, x2) * fx) * fy) * gz +
+                ((D(z2, y1, x1) * gx + D(z2, y1, x2) * fx) * gy + (D(z2, y2, x1) * gx + D(z2, y2, x2) * fx) * fy) * fz;
+    if (!dgrid.empty()) {  // per-voxel directions: value derivative at the point
+        for (int k = 0; k < 8; ++k) {
+            const int dx = k & 1, dy = (k >> 1) & 1, dz = (k >> 2) & 1;
+            const double w = (dx ? fx.v : gx.v) * (dy ? fy.v : gy.v) * (dz ? fz.v : gz.v);
+            const float *q = &dgrid[(((size_t)(z1 + dz) * res[1] + (y1 + dy)) * res[0] + (x1 + dx)) * N];
+            for (int j = 0; j < N; ++j) r.d[j] += w * (double)q[j];
+        }
+    }
+    return r;
 }
 
 template <int N>
@@ -987,11 +996,13 @@ bool Scene<N>::sample_distance_ad(int med, RayAD<N> &ray, const Dual<N> &tmax, c
             // The reference passes ray.org as p_scatter while `ray` is the same object
             // (volpathAD.cpp:164), so intSigT below integrates from the scatter point
             // forward over [0, t]. That aliasing is part of the estimator and is kept.
+            const RayAD<N> ray0 = ray;
             ray.o = p;
             DV3<N> alb = m.albedo_vol.valid ? m.albedo_vol.lookup3_ad(p) : m.albedo;
             Dual<N> sig = m.scale * dens;
             double ist[N];
-            int_sig_t(m, ray, Dual<N>(0.0), Dual<N>(t), rng, ist);
+            int_sig_t(m, (est_flags & DTRT_EST_SCATTER_SEGMENT_FROM_ORIGIN) ? ray0 : ray, Dual<N>(0.0), Dual<N>(t), rng,
+                      ist);
             Dual<N> tmp(1.0);
             for (int j = 0; j < N; ++j) tmp.d[j] = -ist[j];
             thr = cmul(thr, alb * (sig * tmp / sig.v));

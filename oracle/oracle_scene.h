@@ -84,6 +84,9 @@ struct Grid {
     double max_value = 0;
     M4 v2w, w2v;
     V3 trans_vel[N], rot_vel[N];
+    // per-voxel derivative directions [voxel][N] (extension, no reference counterpart):
+    // derivative slot j of lookup_ad gains the trilinear interpolation of direction j
+    std::vector<float> dgrid;
     void configure();
     V3 to_grid(const V3 &pw) const;
     DV3<N> to_grid_ad(const DV3<N> &pw) const;
@@ -202,6 +205,9 @@ struct Scene {
     std::vector<PrimaryEdge<N>> primary_edges;
     Distrib primary_distrb;
     long tracking_cap = 10000;  // heterogeneous.cpp:6
+    // DTRT_EST_SCATTER_SEGMENT_FROM_ORIGIN: integrate the scatter-event derivative over the
+    // segment travelled instead of the reference's aliased one (extension, default off)
+    unsigned est_flags = 0;
 
     std::string build(const dtrt_scene_desc &desc);
     void init_edges(const std::vector<double> &weights);

@@ -14,7 +14,8 @@ LIB_PATH = os.path.join(_HERE, "_build", "libdtrt_gb300.so")
 c_float_p = ctypes.POINTER(ctypes.c_float)
 c_int_p = ctypes.POINTER(ctypes.c_int)
 
-DTRT_OK = 0
+(DTRT_OK, DTRT_ERR_INVALID, DTRT_ERR_CUDA, DTRT_ERR_OVERFLOW, DTRT_ERR_UNSUPPORTED, DTRT_ERR_IO, DTRT_ERR_STEP_CAP,
+ DTRT_ERR_NO_DEVICE) = range(8)
 STATUS_NAMES = {
     0: "OK", 1: "INVALID", 2: "CUDA", 3: "OVERFLOW", 4: "UNSUPPORTED", 5: "IO", 6: "STEP_CAP", 7: "NO_DEVICE",
 }

@@ -690,11 +690,24 @@ DT_D DV<N> grid_point_ad(const DevGrid &g, const DV<N> &pw) {  // gridvolume.h:3
     }
     return p;
 }
+// Cell of the lower trilinear corner, or false when the 2x2x2 stencil leaves the grid
+// (gridvolume.h:152-153: out of range reads as 0). The test runs on the float coordinate,
+// where it is exact for finite values (0 <= floor(x) <= res-2 <=> 0 <= x < res-1) and
+// also rejects NaN and +-inf, which an int conversion would map into range or saturate.
+DT_D bool grid_cell(const DevGrid &g, float3 p, int &x1, int &y1, int &z1) {
+    if (!(p.x >= 0.f && p.x < (float)(g.res[0] - 1) && p.y >= 0.f && p.y < (float)(g.res[1] - 1) && p.z >= 0.f &&
+          p.z < (float)(g.res[2] - 1)))
+        return false;
+    x1 = (int)floorf(p.x);
+    y1 = (int)floorf(p.y);
+    z1 = (int)floorf(p.z);
+    return true;
+}
 DT_D float grid_lookup(const DevGrid &g, float3 pw, Ctr &c) {  // gridvolume.h:144-171
     c.lookups++;
     const float3 p = grid_point(g, pw);
-    const int x1 = (int)floorf(p.x), y1 = (int)floorf(p.y), z1 = (int)floorf(p.z);
-    if (x1 < 0 || x1 + 1 >= g.res[0] || y1 < 0 || y1 + 1 >= g.res[1] || z1 < 0 || z1 + 1 >= g.res[2]) return 0.f;
+    int x1, y1, z1;
+    if (!grid_cell(g, p, x1, y1, z1)) return 0.f;
     const float fx = p.x - x1, fy = p.y - y1, fz = p.z - z1, gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
     const int sx = 1, sy = g.res[0], sz = g.res[0] * g.res[1];
     const float *d = g.data + (size_t)z1 * sz + (size_t)y1 * sy + x1;
@@ -711,8 +724,8 @@ DT_D Df<N> grid_lookup_ad(const DevGrid &g, const DV<N> &pw, Ctr &c) {  // gridv
     if (!g.moving && !voxel_dirs && pw.der_zero(0.f)) return Df<N>(grid_lookup(g, pw.val(), c));
     c.lookups++;
     const DV<N> p = grid_point_ad<N>(g, pw);
-    const int x1 = (int)floorf(p.x.v), y1 = (int)floorf(p.y.v), z1 = (int)floorf(p.z.v);
-    if (x1 < 0 || x1 + 1 >= g.res[0] || y1 < 0 || y1 + 1 >= g.res[1] || z1 < 0 || z1 + 1 >= g.res[2]) return Df<N>(0.f);
+    int x1, y1, z1;
+    if (!grid_cell(g, p.val(), x1, y1, z1)) return Df<N>(0.f);
     const Df<N> fx = p.x - (float)x1, fy = p.y - (float)y1, fz = p.z - (float)z1;
     const Df<N> gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
     const int sx = 1, sy = g.res[0], sz = g.res[0] * g.res[1];
@@ -747,10 +760,13 @@ struct AdjCtx {
     float w;
 };
 DT_D void grid_scatter(const DevGrid &g, float *grad, float3 pw, float w) {
-    if (w == 0.f) return;
+    // a zero weight adds nothing; a non-finite one (a factor whose suffix is zero times an
+    // unbounded segment) would poison the gradient, as a non-finite pixel derivative is
+    // dropped by the forward write rule
+    if (w == 0.f || !isfinite(w)) return;
     const float3 p = grid_point(g, pw);
-    const int x1 = (int)floorf(p.x), y1 = (int)floorf(p.y), z1 = (int)floorf(p.z);
-    if (x1 < 0 || x1 + 1 >= g.res[0] || y1 < 0 || y1 + 1 >= g.res[1] || z1 < 0 || z1 + 1 >= g.res[2]) return;
+    int x1, y1, z1;
+    if (!grid_cell(g, p, x1, y1, z1)) return;
     const float fx = p.x - x1, fy = p.y - y1, fz = p.z - z1, gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
     const int sy = g.res[0], sz = g.res[0] * g.res[1];
     float *q = grad + (size_t)z1 * sz + (size_t)y1 * sy + x1;
@@ -765,9 +781,8 @@ DT_D void grid_scatter(const DevGrid &g, float *grad, float3 pw, float w) {
 }
 DT_D float3 grid_lookup3(const DevGrid &g, float3 pw) {  // gridvolume.h:204-232
     const float3 p = grid_point(g, pw);
-    const int x1 = (int)floorf(p.x), y1 = (int)floorf(p.y), z1 = (int)floorf(p.z);
-    if (x1 < 0 || x1 + 1 >= g.res[0] || y1 < 0 || y1 + 1 >= g.res[1] || z1 < 0 || z1 + 1 >= g.res[2])
-        return mk(0.f, 0.f, 0.f);
+    int x1, y1, z1;
+    if (!grid_cell(g, p, x1, y1, z1)) return mk(0.f, 0.f, 0.f);
     const float fx = p.x - x1, fy = p.y - y1, fz = p.z - z1, gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
     float r[3];
     for (int ch = 0; ch < 3; ++ch) {
@@ -780,8 +795,8 @@ DT_D float3 grid_lookup3(const DevGrid &g, float3 pw) {  // gridvolume.h:204-232
 template <int N>
 DT_D DV<N> grid_lookup3_ad(const DevGrid &g, const DV<N> &pw) {  // gridvolume.h:235-263
     const DV<N> p = grid_point_ad<N>(g, pw);
-    const int x1 = (int)floorf(p.x.v), y1 = (int)floorf(p.y.v), z1 = (int)floorf(p.z.v);
-    if (x1 < 0 || x1 + 1 >= g.res[0] || y1 < 0 || y1 + 1 >= g.res[1] || z1 < 0 || z1 + 1 >= g.res[2]) return DV<N>();
+    int x1, y1, z1;
+    if (!grid_cell(g, p.val(), x1, y1, z1)) return DV<N>();
     const Df<N> fx = p.x - (float)x1, fy = p.y - (float)y1, fz = p.z - (float)z1;
     const Df<N> gx = 1.f - fx, gy = 1.f - fy, gz = 1.f - fz;
     Df<N> r[3];
@@ -867,7 +882,7 @@ DT_HEAVY void int_sig_t(const DevScene &sc, const DevMedium &m, const RayAD<N> &
 #pragma unroll
     for (int j = 0; j < N; ++j) out[j] = 0.f;
     const float len = tmax.v - tmin.v;
-    const bool scatter = adj != nullptr && m.grad_off >= 0;
+    const bool scatter = adj != nullptr && m.grad_off >= 0 && adj->w != 0.f;
     for (int i = 0; i < 10; ++i) {
         const float r = ((float)i + rng.next1()) * 0.1f;
         const Df<N> tt = tmin + len * r;

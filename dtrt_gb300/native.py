@@ -113,10 +113,10 @@ class NativeScene:
         o = kw.pop("options", None) or self.options(**kw)
         vp = ctypes.c_void_p
         if device:
-            _abi.check(self.lib.dtrt_render_adjoint(self.handle, ctypes.byref(o), vp(d_image or 0),
-                                                     vp(image if isinstance(image, int) else 0),
-                                                     vp(density_grad if isinstance(density_grad, int) else 0), None, 1,
-                                                     vp(stream or 0)))
+            def dptr(x):  # a device address given as a plain int; anything else (None, bool) means absent
+                return vp(x) if type(x) is int and x != 0 else None
+            _abi.check(self.lib.dtrt_render_adjoint(self.handle, ctypes.byref(o), dptr(d_image), dptr(image),
+                                                     dptr(density_grad), None, 1, vp(stream or 0)))
             return None
         h, w = self.spec.out_shape()[1:3]
         img = np.zeros((h, w, 3), np.float32) if image else None

@@ -472,23 +472,24 @@ def config2(width=256, height=256, subdiv=5, nder=8, seed=2, displaced=False, si
     return SceneSpec(nder, _camera(width, height, nder=nder), shapes, bsdfs, emitters, [], [], name="C2")
 
 
-def config3(width=512, height=512, res=128, seed=3, nder=8, amp_jitter=None):
+def config3(width=512, height=512, res=128, seed=3, nder=8, amp_jitter=None, param_slots=True, nblobs=32):
     """C3: 128^3 grid of 32 blobs inside a null-bounded unit cube (scale 8, albedo
     0.95, HG 0.5). Forward-mode slots: scale, albedo, g, volume translation x/y/z,
-    volume rotation about y and about x."""
+    volume rotation about y and about x. param_slots=False leaves every slot empty
+    (for per-voxel density directions set on the scene afterwards)."""
     shapes, bsdfs, emitters = [], [], []
     cv, cf = box((-0.5, -0.5, -0.5), (0.5, 0.5, 0.5))
     bsdfs.append(BsdfSpec(_abi.BSDF_NULL))
     shapes.append(ShapeSpec(cv, cf, bsdf_id=0, med_int_id=0))
     _stage(shapes, bsdfs, emitters)
-    grid, _ = blob_grid(res, 32, seed, amp_jitter=amp_jitter)
+    grid, _ = blob_grid(res, nblobs, seed, amp_jitter=amp_jitter)
     d_scale = np.zeros(nder, np.float32)
     d_alb = np.zeros((nder, 3), np.float32)
     d_g = np.zeros(nder, np.float32)
     tv = np.zeros((nder, 3), np.float32)
     rv = np.zeros((nder, 3), np.float32)
     slots = [("scale", None), ("albedo", None), ("g", None), ("tx", 0), ("ty", 1), ("tz", 2), ("ry", 1), ("rx", 0)]
-    for j in range(nder):
+    for j in range(nder if param_slots else 0):
         kind, ax = slots[j % len(slots)]
         if kind == "scale":
             d_scale[j] = 1.0

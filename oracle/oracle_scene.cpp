@@ -218,6 +218,7 @@ DV3<N> Grid<N>::to_grid_ad(const DV3<N> &pw) const {  // gridvolume.h:301-326 (r
 template <int N>
 double Grid<N>::lookup(const V3 &pw) const {  // gridvolume.h:144-171
     V3 p = to_grid(pw);
+    if (!in_cell_range(p.x, p.y, p.z)) return {};
     int x1 = (int)std::floor(p.x), y1 = (int)std::floor(p.y), z1 = (int)std::floor(p.z);
     int x2 = x1 + 1, y2 = y1 + 1, z2 = z1 + 1;
     if (x1 < 0 || x2 >= res[0] || y1 < 0 || y2 >= res[1] || z1 < 0 || z2 >= res[2]) return 0.0;
@@ -230,6 +231,7 @@ double Grid<N>::lookup(const V3 &pw) const {  // gridvolume.h:144-171
 template <int N>
 Dual<N> Grid<N>::lookup_ad(const DV3<N> &pw) const {  // gridvolume.h:174-201
     DV3<N> p = to_grid_ad(pw);
+    if (!in_cell_range(p.x.v, p.y.v, p.z.v)) return {};
     int x1 = (int)std::floor(p.x.v), y1 = (int)std::floor(p.y.v), z1 = (int)std::floor(p.z.v);
     int x2 = x1 + 1, y2 = y1 + 1, z2 = z1 + 1;
     if (x1 < 0 || x2 >= res[0] || y1 < 0 || y2 >= res[1] || z1 < 0 || z2 >= res[2]) return Dual<N>(0.0);
@@ -252,6 +254,7 @@ Dual<N> Grid<N>::lookup_ad(const DV3<N> &pw) const {  // gridvolume.h:174-201
 template <int N>
 V3 Grid<N>::lookup3(const V3 &pw) const {  // gridvolume.h:204-232
     V3 p = to_grid(pw);
+    if (!in_cell_range(p.x, p.y, p.z)) return {};
     int x1 = (int)std::floor(p.x), y1 = (int)std::floor(p.y), z1 = (int)std::floor(p.z);
     int x2 = x1 + 1, y2 = y1 + 1, z2 = z1 + 1;
     if (x1 < 0 || x2 >= res[0] || y1 < 0 || y2 >= res[1] || z1 < 0 || z2 >= res[2]) return V3();
@@ -268,6 +271,7 @@ V3 Grid<N>::lookup3(const V3 &pw) const {  // gridvolume.h:204-232
 template <int N>
 DV3<N> Grid<N>::lookup3_ad(const DV3<N> &pw) const {  // gridvolume.h:235-263
     DV3<N> p = to_grid_ad(pw);
+    if (!in_cell_range(p.x.v, p.y.v, p.z.v)) return {};
     int x1 = (int)std::floor(p.x.v), y1 = (int)std::floor(p.y.v), z1 = (int)std::floor(p.z.v);
     int x2 = x1 + 1, y2 = y1 + 1, z2 = z1 + 1;
     if (x1 < 0 || x2 >= res[0] || y1 < 0 || y2 >= res[1] || z1 < 0 || z2 >= res[2]) return DV3<N>();

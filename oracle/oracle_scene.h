@@ -87,6 +87,11 @@ struct Grid {
     // per-voxel derivative directions [voxel][N] (extension, no reference counterpart):
     // derivative slot j of lookup_ad gains the trilinear interpolation of direction j
     std::vector<float> dgrid;
+    // the 2x2x2 stencil at grid coordinate (x, y, z) lies inside the grid; false for
+    // NaN / inf as well (gridvolume.h:152-153 reads out of range as 0)
+    bool in_cell_range(double x, double y, double z) const {
+        return x >= 0.0 && x < res[0] - 1 && y >= 0.0 && y < res[1] - 1 && z >= 0.0 && z < res[2] - 1;
+    }
     void configure();
     V3 to_grid(const V3 &pw) const;
     DV3<N> to_grid_ad(const DV3<N> &pw) const;

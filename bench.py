@@ -244,16 +244,21 @@ def run_gpu(args, wl_name, rank, world, local_rank):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = alg_bytes / (kms[dom] / args.steps / 1e3) / 1e9 if kms[dom] > 0 else 0.0
+    # DRAM bytes of the dominant kernel per step, from an ncu capture of one launch of it
+    # (per camera path, scaled to the step's paths; the capture's source is recorded)
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get(f"{wl_name}:{dom}")
+    if os.path.exists(tfile) and args.size is None:
+        t = json.load(open(tfile)).get(f"{wl_name}:{dom}")
+        if t:
+            traffic = t["dram_bytes_per_path"] * paths_per_step
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": f"k_{dom}",
                 "peak_source": "measured" if peaks else "fallback",
                 "bytes_per_step": alg_bytes,
                 "bytes_model": "64 B per BVH node visit + 48 B per triangle test + 32 B per trilinear lookup "
-                               "(device counters of one instrumented render)"}
+                               "(device counters of one instrumented render)",
+                "traffic_note": "dram read+write per step scaled from one ncu-captured launch (profiles/traffic.json)"}
     line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
@@ -272,9 +277,216 @@ def run_gpu(args, wl_name, rank, world, local_rank):
                                   "li_tasks": cstats["li_tasks"] / paths_per_step}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(wl_name, args.cpu_seconds_per_step, args.size)
+    if rank == 0 and not args.no_grad_rmse:
+        line["adjoint"] = adjoint_throughput_c3()
+        line["grad_rmse"] = grad_rmse_c3(size=args.grad_size)
     scene.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- gradient accuracy vs time
+def grad_rmse_c3(size=None, runs=16, run_spp=64, ladder_max=64, seed=31):
+    """Time to 1% gradient RMSE on the 128^3-grid volume-density workload (C3: 512x512,
+    depth 16, scale 8, albedo 0.95, HG 0.5): the reverse-mode adjoint (dtrt_render_adjoint,
+    one replay pass gives all 2,097,152 voxel derivatives) against the forward-mode path
+    (dtrt_render_fwd with per-voxel density directions, 8 per pass).
+
+    Quantities: the gradient of an L2 image loss (target: the same grid with +-20% blob
+    amplitudes) along the shapes of 8 of the 32 blobs (the derivatives with respect to
+    those amplitudes) and at 16 random voxels inside the blobs: 24 numbers = 3 forward
+    passes of nder 8, or 1 adjoint pass.
+
+    Both methods trace the same paths for the same seed (the adjoint is the transpose of
+    the forward-mode estimator), so their per-seed estimates coincide (checked on a ladder
+    of runs) and so does the spp at which the relative RMSE sqrt(E||g_s - g||^2) / ||g||
+    reaches 1%. That spp is estimated from `runs` independent adjoint runs at run_spp:
+    E||g_s - g||^2 = tr Cov(g_run) * run_spp / s, with a bootstrap interval. The time of
+    each method is that spp times its measured CUDA-event time per spp."""
+    import torch
+    from dtrt_gb300 import native, scenes
+    W = H = size or 512
+    res, depth = 128, 16
+    spec = scenes.config3(W, H, res=res, nder=8, param_slots=False)
+    tgt = scenes.config3(W, H, res=res, nder=8, param_slots=False, amp_jitter=0.2)
+    grid = spec.media[0].density
+    rng = np.random.default_rng(seed)
+    _, (centres, sigmas, _amps) = scenes.blob_grid(res, 32, 3)  # the generator of config3's grid
+    blobs = np.stack([scenes.blob_field(res, centres[k], sigmas[k]) for k in range(8)])
+    inner = np.zeros_like(grid, bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    vox = rng.choice(np.flatnonzero((grid > 0.2 * grid.max()) & inner), size=16, replace=False)
+    unit = np.zeros((16,) + grid.shape, np.float32)
+    for i, v in enumerate(vox):
+        unit[i].flat[v] = 1.0
+    sets = [blobs.astype(np.float32), unit[:8], unit[8:]]
+    kw = dict(max_bounces=depth, sppe=0, sppse=10)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    fwd_scenes = []
+    for d in sets:
+        sc = native.NativeScene(spec)
+        sc.set_density_derivatives(0, d)
+        fwd_scenes.append(sc)
+    adj_scene = fwd_scenes[0]
+    with native.NativeScene(tgt) as nt:
+        T = nt.render_adjoint(None, image=True, density_grad=False, seed=2, spp=512, **kw)[0]
+    I = adj_scene.render_adjoint(None, image=True, density_grad=False, seed=1, spp=512, **kw)[0]
+    dimg = torch.from_numpy(2.0 * (I - T) / I.size).cuda()
+    dirs_dev = torch.from_numpy(blobs.reshape(8, -1)).cuda()
+    vox_dev = torch.from_numpy(vox).cuda()
+    out = torch.empty(spec.out_shape(), dtype=torch.float32, device="cuda")
+    grad = torch.empty(res ** 3, dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def forward_mode(spp, sd):
+        vals, ms = [], 0.0
+        for sc in fwd_scenes:
+            e0.record(stream)
+            sc.render(out.data_ptr(), stream=sptr, seed=sd, spp=spp, **kw)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+            vals.append((dimg[None] * out[1:]).double().sum(dim=(1, 2, 3)))
+        return torch.cat(vals).cpu().numpy(), ms
+
+    def adjoint(spp, sd):
+        e0.record(stream)
+        adj_scene.render_adjoint(dimg.data_ptr(), image=None, density_grad=grad.data_ptr(), stream=sptr, device=True,
+                                 seed=sd, spp=spp, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        g = grad.double()
+        v = torch.cat([dirs_dev.double() @ g, g[vox_dev]])
+        return v.cpu().numpy(), e0.elapsed_time(e1)
+
+    t0 = time.perf_counter()
+    G = np.stack([adjoint(run_spp, 30000 + r)[0] for r in range(runs)])
+    g_hat = G.mean(0)
+    gn2 = float(g_hat @ g_hat)
+
+    def spp_1pct(Gs):
+        m = Gs.mean(0)
+        return run_spp * float(Gs.var(0, ddof=1).sum()) / (1e-4 * float(m @ m))
+
+    s1 = spp_1pct(G)
+    brng = np.random.default_rng(0)
+    boots = sorted(spp_1pct(G[brng.integers(0, runs, runs)]) for _ in range(200))
+    t_var = time.perf_counter() - t0
+    result = {"workload": f"C3 {W}x{H}, {res}^3 grid, depth {depth}, L2 loss vs +-20% amplitude target",
+              "quantities": "derivatives along 8 blob-amplitude directions + at 16 random voxels (24)",
+              "variance_runs": {"runs": runs, "spp": run_spp, "seconds": t_var,
+                                "rel_se_of_mean": float(np.sqrt(G.var(0, ddof=1).sum() / runs / gn2))},
+              "spp_to_1pct": s1, "spp_to_1pct_bootstrap_90": [boots[10], boots[189]], "threshold": 0.01}
+    ladders = {}
+    for name, fn in (("adjoint", adjoint), ("forward_mode", forward_mode)):
+        ladder, spp = [], 1
+        while spp <= ladder_max:
+            v, ms = fn(spp, 20000 + spp)
+            ladders.setdefault(spp, []).append(v)
+            ladder.append({"spp": spp, "ms": ms, "rel_err_vs_mean": float(np.linalg.norm(v - g_hat) / np.sqrt(gn2))})
+            spp *= 2
+        ms_per_spp = ladder[-1]["ms"] / ladder[-1]["spp"]
+        result[name] = {"ladder": ladder, "ms_per_spp": ms_per_spp, "ms_to_1pct": s1 * ms_per_spp}
+    # same seed, same paths: the two methods' estimates agree run by run
+    result["max_rel_diff_adjoint_vs_forward"] = max(float(np.linalg.norm(a - b) / np.sqrt(gn2))
+                                                    for a, b in ladders.values())
+    a, f = result["adjoint"], result["forward_mode"]
+    result["speedup_time_to_1pct"] = f["ms_to_1pct"] / a["ms_to_1pct"]
+    # all 2,097,152 voxel derivatives by forward mode: one nder-8 pass per 8 voxels
+    per_pass = f["ms_to_1pct"] / len(fwd_scenes)
+    result["forward_mode_full_gradient_s_estimate"] = per_pass * (res ** 3 / 8) / 1e3
+    result["speedup_full_gradient_estimate"] = per_pass * (res ** 3 / 8) / a["ms_to_1pct"]
+    for sc in fwd_scenes:
+        sc.close()
+    return result
+
+
+def adjoint_throughput_c3(steps=3, warmup=1, size=512, spp=128):
+    """Paths/s of the density adjoint (both replay passes) on the C3 workload (512x512,
+    128 spp, depth 16, 128^3 grid), device-resident dL/dI and gradient."""
+    import torch
+    from dtrt_gb300 import native, scenes
+    spec = scenes.config3(size, size, res=128, nder=8, param_slots=False)
+    stream = torch.cuda.current_stream()
+    dimg = torch.randn((size, size, 3), device="cuda") * 1e-3
+    grad = torch.empty(128 ** 3, device="cuda")
+    kw = dict(spp=spp, max_bounces=16, sppe=0, sppse=10)
+    with native.NativeScene(spec) as sc:
+        for k in range(warmup):
+            sc.render_adjoint(dimg.data_ptr(), image=None, density_grad=grad.data_ptr(), stream=stream.cuda_stream,
+                              device=True, seed=900 + k, **kw)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(steps):
+            sc.render_adjoint(dimg.data_ptr(), image=None, density_grad=grad.data_ptr(), stream=stream.cuda_stream,
+                              device=True, seed=k, **kw)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+    return {"workload": f"C3 {size}x{size}, {spp} spp, depth 16, 128^3 grid: full density gradient",
+            "paths_per_s": size * size * spp / (ms / 1e3), "ms_per_pass": ms}
+
+
+def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2):
+    """C4: n seeded scenes of uneven size (1k-50k triangles, half with a 32^3-128^3 grid,
+    128^2-512^2, 16-256 spp, depth 4-16), image + density gradient per scene, as one
+    autotuned persistent launch replayed from a CUDA graph, against the same renders issued
+    one scene at a time (dtrt_render_adjoint per scene) on the same stream."""
+    import torch
+    from dtrt_gb300 import native, scenes
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    items, total_paths = [], 0
+    for i in range(n):
+        spec, kw = scenes.config4(i, side_scale=side_scale, spp_scale=spp_scale)
+        sc = native.NativeScene(spec)
+        opts = sc.options(seed=100 + i, spp=kw["spp"], max_bounces=kw["max_bounces"], sppe=0)
+        nvox = sc.gradient_sizes()[0]
+        h, w = spec.height, spec.width
+        dimg = torch.randn((h, w, 3), device="cuda") * 1e-3
+        img = torch.zeros((h, w, 3), device="cuda")
+        grad = torch.zeros(max(nvox, 1), device="cuda")
+        items.append((sc, opts, dimg, img, grad, nvox))
+        total_paths += h * w * kw["spp"]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def one_at_a_time():
+        for sc, opts, dimg, img, grad, nvox in items:
+            sc.render_adjoint(dimg.data_ptr(), image=img.data_ptr(), density_grad=grad.data_ptr() if nvox else None,
+                              stream=sptr, device=True, options=opts)
+
+    one_at_a_time()  # warm-up
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        one_at_a_time()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1) / reps
+    t0 = time.perf_counter()
+    batch = native.Batch([(sc, opts, dimg.data_ptr(), img.data_ptr(), grad.data_ptr() if nvox else 0)
+                          for sc, opts, dimg, img, grad, nvox in items], autotune=True, graph=True, stream=sptr)
+    tune_s = time.perf_counter() - t0
+    batch.launch(sptr)  # warm-up
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        batch.launch(sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_batch = e0.elapsed_time(e1) / reps
+    st = batch.stats()
+    batch.close()
+    for it in items:
+        it[0].close()
+    return {"workload": f"C4 {n} scenes (side x{side_scale}, spp x{spp_scale}): image + density gradient",
+            "paths": total_paths, "ms_one_at_a_time": ms_seq, "ms_batch": ms_batch,
+            "paths_per_s_batch": total_paths / (ms_batch / 1e3), "speedup": ms_seq / ms_batch,
+            "tune_and_capture_s": tune_s, "chunk_paths": st["chunk_paths"],
+            "order_longest_first": st["order_longest_first"], "grid_blocks": st["grid_blocks"],
+            "trials": st["trials"]}
 
 
 def cpu_baseline(wl_name, target_s, size=None):
@@ -301,10 +513,17 @@ def main():
     ap.add_argument("--cpu-seconds-per-step", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", type=int, default=None, help="image side override for small profiling runs")
+    ap.add_argument("--no-grad-rmse", action="store_true", help="skip the adjoint vs forward-mode gradient leg")
+    ap.add_argument("--grad-size", type=int, default=None, help="image side of the gradient leg (default 512)")
+    ap.add_argument("--adjoint-only", action="store_true", help="time only the C3 density adjoint replay")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.adjoint_only:  # the adjoint replay alone (small profiling runs with --size)
+        print(json.dumps(adjoint_throughput_c3(steps=args.steps, warmup=args.warmup, size=args.size or 512)),
+              flush=True)
+        return
     if args.impl == "reference":
         if rank == 0:
             run_reference(args, args.config, rank)

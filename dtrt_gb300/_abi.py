@@ -134,6 +134,37 @@ class RenderStats(ctypes.Structure):
         return d
 
 
+BATCH_MAX_ITEMS, BATCH_MAX_TRIALS = 256, 16
+BATCH_AUTOTUNE, BATCH_GRAPH = 1, 2
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("opts", RenderOptions), ("d_image", ctypes.c_void_p),
+                ("image", ctypes.c_void_p), ("d_density", ctypes.c_void_p)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [
+        ("num_items", ctypes.c_int), ("total_paths", ctypes.c_uint64), ("grid_blocks", ctypes.c_int),
+        ("blocks_per_sm", ctypes.c_int), ("chunk_paths", ctypes.c_int), ("order_longest_first", ctypes.c_int),
+        ("graph", ctypes.c_int), ("num_trials", ctypes.c_int),
+        ("trial_chunk", ctypes.c_int * BATCH_MAX_TRIALS), ("trial_order", ctypes.c_int * BATCH_MAX_TRIALS),
+        ("trial_ms", ctypes.c_float * BATCH_MAX_TRIALS), ("tune_sample_stride", ctypes.c_int64),
+        ("item_ms_estimate", ctypes.c_double * BATCH_MAX_ITEMS), ("order", ctypes.c_int * BATCH_MAX_ITEMS),
+    ]
+
+    def as_dict(self):
+        n, t = self.num_items, self.num_trials
+        return {"num_items": n, "total_paths": self.total_paths, "grid_blocks": self.grid_blocks,
+                "blocks_per_sm": self.blocks_per_sm, "chunk_paths": self.chunk_paths,
+                "order_longest_first": bool(self.order_longest_first), "graph": bool(self.graph),
+                "trials": [{"chunk": self.trial_chunk[i], "order": "longest_first" if self.trial_order[i] == 0
+                            else "input", "ms": self.trial_ms[i]} for i in range(t)],
+                "tune_sample_stride": self.tune_sample_stride,
+                "item_ms_estimate": list(self.item_ms_estimate[:min(n, BATCH_MAX_ITEMS)]),
+                "order": list(self.order[:min(n, BATCH_MAX_ITEMS)])}
+
+
 # Every C-ABI symbol declared in include/dtrt_gb300.h, with its ctypes signature.
 EST_SCATTER_SEGMENT_FROM_ORIGIN = 1
 
@@ -161,6 +192,11 @@ _SIGNATURES = {
     "dtrt_render_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_void_p]),
+    "dtrt_batch_create": (ctypes.c_int, [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_uint, ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "dtrt_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dtrt_batch_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchStats)]),
+    "dtrt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dtrt_trace_closest": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int, c_int_p, c_float_p]),
     "dtrt_vol_read": (ctypes.c_int, [ctypes.c_char_p, c_int_p, c_int_p, c_float_p, c_float_p, c_float_p]),
 }

@@ -192,18 +192,15 @@ DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, 
     return acc;
 }
 
-// One thread per camera path: pass A (value), then pass B (scatter) when the path and its
-// pixel's dL/dI are non-zero. img_acc (optional) receives the image, FP64 [npix][3].
+// One camera path (index gi of the launch's range): pass A (value), then pass B (scatter)
+// when the path and its pixel's dL/dI are non-zero. img_acc (optional) receives the image,
+// FP64 [npix][3]. Contains warp collectives: all 32 lanes of a warp must call it together.
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp, const float *dimg, float *grad,
-                                                    double *img_acc, unsigned long long *ctr) {
-    __shared__ int s_stack[kStackDepth * kBlock];
-    int *stack = s_stack + threadIdx.x;
-    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+DT_D void adjoint_one(const DevScene &sc, const RenderParams &rp, int *stack, long long gi, const float *dimg,
+                      float *grad, double *img_acc, Ctr &c) {
     const bool active = gi < rp.path_count;
     const long long g = rp.path_begin + (active ? gi : 0);
     const int pixel = (int)(g / rp.spp);
-    Ctr c;
     AdjCtx adj{grad, 0.f};
     float3 total = mk(0.f, 0.f, 0.f);
     if (active) {
@@ -226,11 +223,20 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp
             for (int k = 0; k < 3; ++k)
                 if (v[k] != 0.f) atomicAdd(img_acc + (size_t)pixel * 3 + k, (double)v[k]);
     }
+}
+
+// One thread per camera path of one scene.
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp, const float *dimg, float *grad,
+                                                    double *img_acc, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    Ctr c;
+    adjoint_one<N>(sc, rp, s_stack + threadIdx.x, (long long)blockIdx.x * kBlock + threadIdx.x, dimg, grad, img_acc, c);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
 // Image write rule of integratorAD.cpp:59-87 (a pixel is written only if non-negative).
-__global__ void k_adjoint_image(int npix, const double *acc, float *out) {
+static __global__ void k_adjoint_image(int npix, const double *acc, float *out) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
     const double *a = acc + (size_t)p * 3;

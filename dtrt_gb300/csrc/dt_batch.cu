@@ -1,0 +1,478 @@
+// dtrt_gb300 — many scenes of uneven size in one persistent launch under a CUDA graph.
+//
+// No counterpart in the reference (one scene per blocking render call,
+// integratorAD.cpp:19-166, parallel over pixels of that scene only). Every item of a batch
+// is one scene with its own render options and device buffers; the work is the density
+// adjoint replay of dtrt_render_adjoint (image + density gradient) for each item.
+//
+// Work distribution: the camera paths of all items are cut into chunks of `chunk` paths
+// (a multiple of 32), laid out item after item in a tuned item order. A persistent grid
+// (resident blocks only) lets each warp take the next chunk from one global counter, so
+// long and short scenes share the GPU until the last chunk; the item of a chunk is a
+// binary search over the chunk prefix. The launch and its memsets are captured once in a
+// CUDA graph; dtrt_batch_launch replays it.
+//
+// Autotuner: (1) a probe launch per item on a sample of its paths measures the cost per
+// path; items are then ordered longest-total-cost first (or kept in input order, whichever
+// times faster); (2) the chunk size is chosen among 32..512 paths by timing the whole batch
+// on a strided sample of every item's paths.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "dt_adjoint.cuh"
+#include "dt_host.h"
+
+namespace dt {
+
+struct BatchItemDev {
+    DevScene sc;
+    RenderParams rp;
+    const float *dimg;
+    float *grad;
+    double *img_acc;
+};
+
+// chunk c belongs to the item at position i of the order with cbeg[i] <= c < cbeg[i+1]
+__global__ void __launch_bounds__(kBlock) k_batch(const BatchItemDev *items, const long long *cbeg, const int *order,
+                                                  int n, long long total_chunks, int chunk, long long sample_stride,
+                                                  unsigned long long *next) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long c = 0;
+        if (lane == 0) c = atomicAdd(next, 1ull);
+        c = __shfl_sync(full, c, 0);
+        if (c >= (unsigned long long)total_chunks) break;
+        int lo = 0, hi = n - 1;  // largest i with cbeg[i] <= c
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if ((unsigned long long)cbeg[mid] <= c) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchItemDev &it = items[order[lo]];
+        const long long base = ((long long)c - cbeg[lo]) * chunk;
+        Ctr ctr;
+        for (int k = lane; k < chunk; k += 32) {
+            // sample_stride > 1 (tuning): every stride-th path of the item, same layout
+            const long long gi = (base + k) * sample_stride;
+            adjoint_one<1>(it.sc, it.rp, stack, gi, it.dimg, it.grad, it.img_acc, ctr);
+        }
+    }
+}
+
+// FP64 image accumulators -> float images of every item (integratorAD.cpp:59-87 write rule)
+struct BatchImageDev {
+    const double *acc;
+    float *out;
+    long long pix_begin;
+};
+__global__ void k_batch_image(const BatchImageDev *imgs, int n, long long total_pix) {
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= total_pix) return;
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (imgs[mid].pix_begin <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    const long long q = p - imgs[lo].pix_begin;
+    const double *a = imgs[lo].acc + q * 3;
+    const bool nonneg = a[0] >= 0.0 && a[1] >= 0.0 && a[2] >= 0.0;
+    for (int c = 0; c < 3; ++c) imgs[lo].out[q * 3 + c] = nonneg ? (float)a[c] : 0.f;
+}
+
+}  // namespace dt
+
+struct dtrt_batch {
+    int device = 0;
+    int n = 0;
+    std::vector<dtrt_batch_item> items;
+    std::vector<dt::BatchItemDev> host_items;
+    std::vector<size_t> npix, nvox;
+    std::vector<long long> paths;
+    // device memory
+    dt::BatchItemDev *d_items = nullptr;
+    long long *d_cbeg = nullptr;
+    int *d_order = nullptr;
+    dt::BatchImageDev *d_imgs = nullptr;
+    unsigned long long *d_next = nullptr;
+    unsigned int *d_err = nullptr;
+    std::vector<double *> img_acc;
+    // launch shape
+    int grid = 0, chunk = 128, n_img = 0;
+    long long total_chunks = 0, total_pix = 0;
+    std::vector<int> order;
+    std::vector<long long> cbeg;
+    // graph
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    dtrt_batch_stats stats{};
+};
+
+namespace dt {
+namespace {
+
+#define DT_BCK(call)                                                                 \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            set_last_error(std::string(#call) + ": " + cudaGetErrorString(e_));      \
+            return DTRT_ERR_CUDA;                                                    \
+        }                                                                            \
+    } while (0)
+
+void free_batch(dtrt_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    void *ptrs[] = {b->d_items, b->d_cbeg, b->d_order, b->d_imgs, b->d_next, b->d_err};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (double *p : b->img_acc)
+        if (p) cudaFree(p);
+}
+
+// chunk layout for an item order and chunk size (sample_stride > 1: sampled path counts)
+void layout(dtrt_batch *b, const std::vector<int> &order, int chunk, long long stride, std::vector<long long> &cbeg,
+            long long &total) {
+    cbeg.assign(b->n + 1, 0);
+    for (int i = 0; i < b->n; ++i) {
+        const long long p = (b->paths[order[i]] + stride - 1) / stride;
+        cbeg[i + 1] = cbeg[i] + (p + chunk - 1) / chunk;
+    }
+    total = cbeg[b->n];
+}
+
+// upload a chunk layout (blocking copies: never inside a stream capture)
+int upload_layout(dtrt_batch *b, const std::vector<int> &order, int chunk, long long stride, long long &total) {
+    std::vector<long long> cbeg;
+    layout(b, order, chunk, stride, cbeg, total);
+    DT_BCK(cudaMemcpy(b->d_cbeg, cbeg.data(), cbeg.size() * 8, cudaMemcpyHostToDevice));
+    DT_BCK(cudaMemcpy(b->d_order, order.data(), order.size() * 4, cudaMemcpyHostToDevice));
+    return DTRT_OK;
+}
+
+// counter reset + one k_batch launch over the uploaded layout; the caller zeroes outputs
+int launch_kernel(dtrt_batch *b, long long total, int chunk, long long stride, cudaStream_t st) {
+    DT_BCK(cudaMemsetAsync(b->d_next, 0, 8, st));
+    if (total > 0) k_batch<<<b->grid, kBlock, 0, st>>>(b->d_items, b->d_cbeg, b->d_order, b->n, total, chunk, stride, b->d_next);
+    DT_BCK(cudaGetLastError());
+    return DTRT_OK;
+}
+
+int launch_once(dtrt_batch *b, const std::vector<int> &order, int chunk, long long stride, cudaStream_t st) {
+    long long total = 0;
+    DT_BCK(cudaStreamSynchronize(st));  // the layout buffers may still be read by a previous launch
+    int rc = upload_layout(b, order, chunk, stride, total);
+    return rc ? rc : launch_kernel(b, total, chunk, stride, st);
+}
+
+int zero_outputs(dtrt_batch *b, cudaStream_t st) {
+    for (int i = 0; i < b->n; ++i) {
+        if (b->host_items[i].img_acc) DT_BCK(cudaMemsetAsync(b->host_items[i].img_acc, 0, b->npix[i] * 3 * 8, st));
+        if (b->host_items[i].grad) DT_BCK(cudaMemsetAsync(b->host_items[i].grad, 0, b->nvox[i] * 4, st));
+    }
+    DT_BCK(cudaMemsetAsync(b->d_err, 0, 4, st));
+    return DTRT_OK;
+}
+
+// time fn() on st with events (ms)
+template <class F>
+int timed(cudaStream_t st, F &&fn, float &ms) {
+    cudaEvent_t e0, e1;
+    DT_BCK(cudaEventCreate(&e0));
+    DT_BCK(cudaEventCreate(&e1));
+    cudaEventRecord(e0, st);
+    int rc = fn();
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (e != cudaSuccess) {
+        set_last_error(std::string("batch timing: ") + cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
+    }
+    return DTRT_OK;
+}
+
+int autotune(dtrt_batch *b, cudaStream_t st) {
+    const long long kProbePaths = 16384;
+    // (1) cost per path of every item, from a strided probe of about kProbePaths paths
+    std::vector<double> cost(b->n, 0.0);
+    for (int i = 0; i < b->n; ++i) {
+        const long long stride = std::max<long long>(1, b->paths[i] / kProbePaths);
+        std::vector<int> one = {i};
+        // a one-item layout: other items get no chunks
+        std::vector<long long> cbeg = {0, ((b->paths[i] + stride - 1) / stride + 127) / 128};
+        float ms = 0.f;
+        DT_BCK(cudaStreamSynchronize(st));
+        DT_BCK(cudaMemcpy(b->d_cbeg, cbeg.data(), 16, cudaMemcpyHostToDevice));
+        DT_BCK(cudaMemcpy(b->d_order, one.data(), 4, cudaMemcpyHostToDevice));
+        int rc = timed(st, [&]() -> int {
+            DT_BCK(cudaMemsetAsync(b->d_next, 0, 8, st));
+            k_batch<<<b->grid, kBlock, 0, st>>>(b->d_items, b->d_cbeg, b->d_order, 1, cbeg[1], 128, stride, b->d_next);
+            DT_BCK(cudaGetLastError());
+            return DTRT_OK;
+        }, ms);
+        if (rc) return rc;
+        const double sampled = (double)((b->paths[i] + stride - 1) / stride);
+        cost[i] = ms / std::max(1.0, sampled) * (double)b->paths[i];  // ms for the whole item
+        b->stats.item_ms_estimate[std::min(i, DTRT_BATCH_MAX_ITEMS - 1)] = cost[i];
+    }
+    std::vector<int> natural(b->n), longest(b->n);
+    std::iota(natural.begin(), natural.end(), 0);
+    std::iota(longest.begin(), longest.end(), 0);
+    std::stable_sort(longest.begin(), longest.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    // (2) chunk size x order on a strided sample of the whole batch
+    long long total_paths = 0;
+    for (long long p : b->paths) total_paths += p;
+    const long long stride = std::max<long long>(1, total_paths / (1ll << 22));
+    const int chunks[] = {32, 64, 128, 256, 512};
+    float best = 1e30f;
+    int trial = 0;
+    for (int oi = 0; oi < 2; ++oi) {
+        const std::vector<int> &ord = oi == 0 ? longest : natural;
+        for (int ch : chunks) {
+            float ms = 0.f;
+            long long total = 0;
+            DT_BCK(cudaStreamSynchronize(st));
+            int rc = upload_layout(b, ord, ch, stride, total);
+            if (rc) return rc;
+            rc = timed(st, [&]() { return launch_kernel(b, total, ch, stride, st); }, ms);
+            if (rc) return rc;
+            if (trial < DTRT_BATCH_MAX_TRIALS) {
+                b->stats.trial_chunk[trial] = ch;
+                b->stats.trial_order[trial] = oi;
+                b->stats.trial_ms[trial] = ms;
+            }
+            ++trial;
+            if (ms < best) {
+                best = ms;
+                b->chunk = ch;
+                b->order = ord;
+                b->stats.order_longest_first = oi == 0;
+            }
+        }
+    }
+    b->stats.num_trials = std::min(trial, DTRT_BATCH_MAX_TRIALS);
+    b->stats.tune_sample_stride = stride;
+    return DTRT_OK;
+}
+
+// capture zero + launch + image conversion into a graph (the layout is uploaded first and
+// stays fixed: every replay runs the tuned order and chunk size)
+int capture(dtrt_batch *b) {
+    cudaStream_t cs = b->cap_stream;
+    long long total = 0;
+    int rc = upload_layout(b, b->order, b->chunk, 1, total);
+    if (rc) return rc;
+    DT_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    rc = zero_outputs(b, cs);
+    if (!rc) rc = launch_kernel(b, total, b->chunk, 1, cs);
+    if (!rc && b->n_img > 0) {
+        k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, cs>>>(b->d_imgs, b->n_img, b->total_pix);
+        if (cudaGetLastError() != cudaSuccess) rc = DTRT_ERR_CUDA;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(cs, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) {
+        set_last_error(std::string("batch graph capture: ") + cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
+    }
+    b->graph = g;
+    DT_BCK(cudaGraphInstantiate(&b->exec, g, 0));
+    return DTRT_OK;
+}
+
+}  // namespace
+}  // namespace dt
+
+extern "C" {
+
+int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void *stream, dtrt_batch **out) {
+    using namespace dt;
+    if (!items || !out || n <= 0) {
+        set_last_error("null argument or empty batch");
+        return DTRT_ERR_INVALID;
+    }
+    *out = nullptr;
+    std::unique_ptr<dtrt_batch, void (*)(dtrt_batch *)> b(new dtrt_batch(), [](dtrt_batch *p) {
+        free_batch(p);
+        delete p;
+    });
+    cudaStream_t st = (cudaStream_t)stream;
+    b->n = n;
+    b->items.assign(items, items + n);
+    cudaGetDevice(&b->device);
+    DT_BCK(cudaMalloc(&b->d_err, 4));
+    for (int i = 0; i < n; ++i) {
+        const dtrt_batch_item &it = items[i];
+        if (!it.scene || it.opts.spp < 0 || it.opts.max_bounces < 0 || (!it.image && !it.d_density)) {
+            set_last_error("batch item " + std::to_string(i) + ": needs a scene, spp/max_bounces >= 0 and an output");
+            return DTRT_ERR_INVALID;
+        }
+        if (it.scene->device != b->device) {
+            set_last_error("batch items must live on the current device");
+            return DTRT_ERR_INVALID;
+        }
+        if (it.d_density && !it.d_image) {
+            set_last_error("batch item " + std::to_string(i) + ": d_density needs d_image");
+            return DTRT_ERR_INVALID;
+        }
+        DevScene sc = it.scene->dev;
+        sc.vert_der = nullptr;
+        sc.face_n_der = nullptr;
+        sc.normal_der = nullptr;
+        sc.moving_geometry = 0;
+        std::memset(sc.cam.d_cpos, 0, sizeof(sc.cam.d_cpos));
+        std::memset(sc.cam.d_cframe, 0, sizeof(sc.cam.d_cframe));
+        sc.error_flags = b->d_err;
+        const DevCamera &cam = sc.cam;
+        const bool cropped = cam.crop_w > 0 && cam.crop_h > 0;
+        RenderParams rp{};
+        rp.seed = it.opts.seed;
+        rp.spp = it.opts.spp;
+        rp.max_bounces = it.opts.max_bounces;
+        rp.mode = it.opts.mode >= 0 ? it.opts.mode : MODE_ALL;
+        rp.jitter = it.opts.sppe >= 0 ? 1 : 0;
+        rp.ddist = it.opts.ddist_coeff;
+        rp.inv_spp = it.opts.spp > 0 ? 1.0f / (float)it.opts.spp : 0.f;
+        rp.out_w = cropped ? cam.crop_w : cam.width;
+        rp.out_h = cropped ? cam.crop_h : cam.height;
+        rp.crop_x = cropped ? cam.crop_x : 0;
+        rp.crop_y = cropped ? cam.crop_y : 0;
+        rp.npix = rp.out_w * rp.out_h;
+        const long long paths = (long long)rp.npix * std::max(0, it.opts.spp);
+        rp.path_begin = 0;
+        rp.path_count = paths;
+        BatchItemDev d{};
+        d.sc = sc;
+        d.rp = rp;
+        d.dimg = it.d_image;
+        d.grad = (it.d_density && it.scene->density_voxels > 0) ? it.d_density : nullptr;
+        d.img_acc = nullptr;
+        double *acc = nullptr;
+        if (it.image) {
+            DT_BCK(cudaMalloc(&acc, (size_t)rp.npix * 3 * 8));
+            d.img_acc = acc;
+        }
+        b->img_acc.push_back(acc);
+        b->host_items.push_back(d);
+        b->npix.push_back((size_t)rp.npix);
+        b->nvox.push_back((size_t)it.scene->density_voxels);
+        b->paths.push_back(paths);
+    }
+    DT_BCK(cudaMalloc(&b->d_items, sizeof(BatchItemDev) * n));
+    DT_BCK(cudaMemcpy(b->d_items, b->host_items.data(), sizeof(BatchItemDev) * n, cudaMemcpyHostToDevice));
+    DT_BCK(cudaMalloc(&b->d_cbeg, 8 * (n + 1)));
+    DT_BCK(cudaMalloc(&b->d_order, 4 * n));
+    DT_BCK(cudaMalloc(&b->d_next, 8));
+    std::vector<BatchImageDev> imgs;
+    long long pix = 0;
+    for (int i = 0; i < n; ++i)
+        if (items[i].image) {
+            imgs.push_back({b->img_acc[i], items[i].image, pix});
+            pix += (long long)b->npix[i];
+        }
+    b->n_img = (int)imgs.size();
+    b->total_pix = pix;
+    if (!imgs.empty()) {
+        DT_BCK(cudaMalloc(&b->d_imgs, sizeof(BatchImageDev) * imgs.size()));
+        DT_BCK(cudaMemcpy(b->d_imgs, imgs.data(), sizeof(BatchImageDev) * imgs.size(), cudaMemcpyHostToDevice));
+    }
+    // persistent grid: resident blocks only
+    int sms = 0, per_sm = 0;
+    DT_BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+    DT_BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBlock, 0));
+    b->grid = std::max(1, sms * std::max(1, per_sm));
+    b->order.resize(n);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    b->chunk = 128;
+    b->stats.grid_blocks = b->grid;
+    b->stats.blocks_per_sm = per_sm;
+    if (flags & DTRT_BATCH_AUTOTUNE) {
+        int rc = autotune(b.get(), st);
+        if (rc) return rc;
+        DT_BCK(cudaStreamSynchronize(st));
+    }
+    b->stats.chunk_paths = b->chunk;
+    for (int i = 0; i < n && i < DTRT_BATCH_MAX_ITEMS; ++i) b->stats.order[i] = b->order[i];
+    b->stats.num_items = n;
+    long long tp = 0;
+    for (long long p : b->paths) tp += p;
+    b->stats.total_paths = (uint64_t)tp;
+    std::vector<long long> cbeg;
+    long long total = 0;
+    layout(b.get(), b->order, b->chunk, 1, cbeg, total);
+    b->total_chunks = total;
+    if (flags & DTRT_BATCH_GRAPH) {
+        DT_BCK(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+        int rc = capture(b.get());
+        if (rc) return rc;
+        b->stats.graph = 1;
+    }
+    *out = b.release();
+    return DTRT_OK;
+}
+
+int dtrt_batch_launch(dtrt_batch *b, void *stream) {
+    using namespace dt;
+    if (!b) {
+        set_last_error("null batch");
+        return DTRT_ERR_INVALID;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (b->exec) {
+        DT_BCK(cudaGraphLaunch(b->exec, st));
+    } else {
+        int rc = zero_outputs(b, st);
+        if (!rc) rc = launch_once(b, b->order, b->chunk, 1, st);
+        if (rc) return rc;
+        if (b->n_img > 0) {
+            k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, st>>>(b->d_imgs, b->n_img, b->total_pix);
+            DT_BCK(cudaGetLastError());
+        }
+    }
+    unsigned int herr = 0;
+    DT_BCK(cudaMemcpyAsync(&herr, b->d_err, 4, cudaMemcpyDeviceToHost, st));
+    DT_BCK(cudaStreamSynchronize(st));
+    if (herr & ERR_STACK) {
+        set_last_error("BVH traversal stack overflow");
+        return DTRT_ERR_INVALID;
+    }
+    if (herr & ERR_TRACK_CAP) {
+        set_last_error("a delta/ratio tracking loop hit its iteration cap");
+        return DTRT_ERR_STEP_CAP;
+    }
+    return DTRT_OK;
+}
+
+int dtrt_batch_stats_get(const dtrt_batch *b, dtrt_batch_stats *out) {
+    if (!b || !out) {
+        dt::set_last_error("null argument");
+        return DTRT_ERR_INVALID;
+    }
+    *out = b->stats;
+    return DTRT_OK;
+}
+
+int dtrt_batch_destroy(dtrt_batch *b) {
+    if (!b) return DTRT_OK;
+    dt::free_batch(b);
+    delete b;
+    return DTRT_OK;
+}
+
+}  // extern "C"

@@ -60,7 +60,9 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         return DTRT_ERR_CUDA;
     if (!out_on_device && !ensure_buffer((void **)&sb.out, &sb.out_n, out_n * 4)) return DTRT_ERR_CUDA;
     const uint64_t li_cap = s->queue_cap ? s->queue_cap : (uint64_t)24 << 20;
-    const uint64_t rec_cap = s->queue_cap ? s->queue_cap : (uint64_t)4 << 20;
+    // 16 Mi records bound a camera batch at 16Mi/(max_bounces+1) paths (1.5 M at depth 10):
+    // few launches, so the partial last wave of each batch costs little
+    const uint64_t rec_cap = s->queue_cap ? s->queue_cap : (uint64_t)16 << 20;
     if (!ensure_buffer(&sb.qli, &sb.qli_bytes, li_cap * sizeof(LiTask<N>)) ||
         !ensure_buffer(&sb.qe, &sb.qe_bytes, rec_cap * sizeof(EdgeRec<N>)) ||
         !ensure_buffer(&sb.ql, &sb.ql_bytes, rec_cap * sizeof(LinsRec<N>)))

@@ -142,5 +142,46 @@ class NativeScene:
         return hits, t
 
 
+class Batch:
+    """Many scenes in one persistent launch (dtrt_batch_create / _launch / _destroy).
+
+    items: list of (NativeScene, options, d_image_ptr, image_ptr, d_density_ptr) with
+    device pointers as ints (0 = none). The scenes and buffers must outlive the batch."""
+
+    def __init__(self, items, autotune=True, graph=True, stream=None):
+        self.lib = _abi.load()
+        self.scenes = [it[0] for it in items]  # keep the scenes alive
+        arr = (_abi.BatchItem * len(items))()
+        for i, (sc, opts, dimg, img, dden) in enumerate(items):
+            arr[i].scene = sc.handle.value
+            arr[i].opts = opts
+            arr[i].d_image = dimg or None
+            arr[i].image = img or None
+            arr[i].d_density = dden or None
+        flags = (_abi.BATCH_AUTOTUNE if autotune else 0) | (_abi.BATCH_GRAPH if graph else 0)
+        h = ctypes.c_void_p()
+        _abi.check(self.lib.dtrt_batch_create(arr, len(items), flags, ctypes.c_void_p(stream or 0), ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self, stream=None):
+        _abi.check(self.lib.dtrt_batch_launch(self.handle, ctypes.c_void_p(stream or 0)))
+
+    def stats(self):
+        st = _abi.BatchStats()
+        _abi.check(self.lib.dtrt_batch_stats_get(self.handle, ctypes.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.dtrt_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def device_count():
     return _abi.load().dtrt_device_count()

@@ -62,3 +62,55 @@ class ADLossFunc(torch.autograd.Function):
             if i < lvl - 1:
                 g = downsample(g)
         return (None, None, None, ret, None, None, None, None, None, None)
+
+
+class DensityRenderFunc(torch.autograd.Function):
+    """The image of a scene as a differentiable function of one heterogeneous medium's
+    density grid (no counterpart in the reference, whose derivatives are nder-wide
+    forward-mode duals only).
+
+    forward(density, scene, medium_id, options, backward_seed=None) -> image [H, W, 3]
+        uploads `density` ([rz, ry, rx], any device) into the scene
+        (dtrt_scene_set_density) and renders the image of `options`;
+    backward(dL/dimage) -> dL/ddensity
+        the reverse-mode adjoint (dtrt_render_adjoint): every camera path is replayed
+        from its seed, nothing is stored between the two calls. The replay uses
+        `backward_seed` (default options.seed + 1) so that the gradient of a loss that is
+        non-linear in the image is not correlated with the image estimate.
+
+    `scene` is a dtrt_gb300.native.NativeScene.
+    """
+
+    @staticmethod
+    def forward(ctx, density, scene, medium_id, options, backward_seed=None):
+        import numpy as np
+        from .. import _abi
+        dens = density.detach().to("cpu", torch.float32).contiguous().numpy()
+        scene.set_density(medium_id, dens)
+        img, _ = scene.render_adjoint(None, image=True, density_grad=False, options=options)
+        ctx.scene, ctx.medium_id = scene, medium_id
+        ctx.shape, ctx.device = density.shape, density.device
+        o = options
+        seed = o.seed + 1 if backward_seed is None else backward_seed
+        ctx.bwd_options = _abi.RenderOptions(seed, o.spp, o.max_bounces, o.sppe, o.sppse, o.quiet, o.mode, o.ddist_coeff)
+        # voxel offset of this medium in the concatenated gradient
+        off = 0
+        for m in scene.spec.media[:medium_id]:
+            if m.type == _abi.MEDIUM_HETEROGENEOUS:
+                if m.density is not None:
+                    off += int(np.prod(np.asarray(m.density).shape[:3]))
+                else:
+                    from ..scenes import read_vol
+                    off += int(np.prod(read_vol(m.density_file)[0].shape[:3]))
+        ctx.offset = off
+        return torch.from_numpy(img).to(density.device)
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        g = grad_image.detach().to("cpu", torch.float32).contiguous().numpy()
+        _, grad = ctx.scene.render_adjoint(g, image=False, density_grad=True, options=ctx.bwd_options)
+        n = 1
+        for s in ctx.shape:
+            n *= s
+        gd = torch.from_numpy(grad[ctx.offset:ctx.offset + n].reshape(tuple(ctx.shape))).to(ctx.device)
+        return gd, None, None, None, None

@@ -135,6 +135,16 @@ def blob_grid(res, nblobs, seed, amp_range=(0.5, 1.0), sigma_range=(0.05, 0.15),
     return grid.astype(np.float32), (centres, sigmas, amps)
 
 
+def blob_field(res, centre, sigma):
+    """One unit-amplitude Gaussian blob of blob_grid on the same vertices: the derivative
+    of the grid with respect to that blob's amplitude."""
+    x = np.linspace(0.0, 1.0, res)
+    gz = np.exp(-((x - centre[2]) ** 2) / (2 * sigma * sigma))
+    gy = np.exp(-((x - centre[1]) ** 2) / (2 * sigma * sigma))
+    gx = np.exp(-((x - centre[0]) ** 2) / (2 * sigma * sigma))
+    return (gz[:, None, None] * gy[None, :, None] * gx[None, None, :]).astype(np.float32)
+
+
 def write_vol(path, grid, vmin, vmax):
     """Mitsuba VOL v3: 'VOL', version 3, type 1 (float32), res xyz, channels,
     bounds min/max, data z-major with x fastest (gridvolume.h:88-132)."""
@@ -508,13 +518,14 @@ def config3(width=512, height=512, res=128, seed=3, nder=8, amp_jitter=None, par
     return SceneSpec(nder, _camera(width, height, nder=nder), shapes, bsdfs, emitters, phases, media, name="C3")
 
 
-def config4(index, seed=4, nder=1):
+def config4(index, seed=4, nder=1, side_scale=1.0, spp_scale=1.0):
     """One of the 64 uneven C4 scenes: an icosphere or a displaced plane of
-    1k-50k triangles (log-uniform), 50% with a 32^3-128^3 blob grid."""
+    1k-50k triangles (log-uniform), 50% with a 32^3-128^3 blob grid. Image side
+    128-512 and spp 16-256 (both scaled down by side_scale / spp_scale for small tests)."""
     rng = np.random.default_rng([seed, index])
     ntri = int(math.exp(rng.uniform(math.log(1000), math.log(50000))))
-    side = int(rng.choice([128, 192, 256, 384, 512]))
-    spp = int(2 ** rng.integers(4, 9))
+    side = max(8, int(int(rng.choice([128, 192, 256, 384, 512])) * side_scale))
+    spp = max(1, int(int(2 ** rng.integers(4, 9)) * spp_scale))
     depth = int(rng.integers(4, 17))
     shapes, bsdfs, emitters, media, phases = [], [], [], [], []
     if rng.uniform() < 0.5:

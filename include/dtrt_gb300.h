@@ -309,6 +309,53 @@ int dtrt_scene_set_density_derivatives(dtrt_scene *scene, int medium_id, const f
 int dtrt_render_adjoint(dtrt_scene *scene, const dtrt_render_options *opts, const float *d_image, float *image,
                         float *d_density, float *d_vertices, int on_device, void *stream);
 
+/* ---------------------------------------------------------------- batches of scenes
+ * No counterpart in the reference, which renders one scene per blocking call
+ * (integratorAD.cpp:19-166). A batch is a fixed list of scenes with their own options and
+ * device buffers, rendered together as one persistent launch: the image and, where a
+ * scene has density grids and d_image is given, the density adjoint of each item (the
+ * work of dtrt_render_adjoint). Paths of all items are cut into chunks that warps take
+ * from one counter; the item order and chunk size are autotuned; the launch is captured
+ * in a CUDA graph that dtrt_batch_launch replays. The items' buffers are borrowed for the
+ * batch's lifetime and are rewritten by every launch. */
+typedef struct {
+    dtrt_scene *scene;
+    dtrt_render_options opts;  /* seed, spp, max_bounces, sppe (< 0: no pixel jitter), mode */
+    const float *d_image;      /* NULL or device [H][W][3] dL/dI (needed with d_density) */
+    float *image;              /* NULL or device [H][W][3] */
+    float *d_density;          /* NULL or device [density_voxels] */
+} dtrt_batch_item;
+
+#define DTRT_BATCH_AUTOTUNE 1u /* measure item costs and pick item order and chunk size */
+#define DTRT_BATCH_GRAPH 2u    /* capture the launch in a CUDA graph */
+#define DTRT_BATCH_MAX_ITEMS 256
+#define DTRT_BATCH_MAX_TRIALS 16
+
+typedef struct {
+    int num_items;
+    uint64_t total_paths;
+    int grid_blocks, blocks_per_sm; /* persistent grid: resident blocks only */
+    int chunk_paths;                /* paths a warp takes per counter increment */
+    int order_longest_first;        /* 1: items ordered by measured cost, longest first */
+    int graph;                      /* 1: launches replay a CUDA graph */
+    int num_trials;
+    int trial_chunk[DTRT_BATCH_MAX_TRIALS], trial_order[DTRT_BATCH_MAX_TRIALS];
+    float trial_ms[DTRT_BATCH_MAX_TRIALS]; /* tuning launches on a strided path sample */
+    int64_t tune_sample_stride;
+    double item_ms_estimate[DTRT_BATCH_MAX_ITEMS]; /* measured cost of each item (probe) */
+    int order[DTRT_BATCH_MAX_ITEMS];
+} dtrt_batch_stats;
+
+typedef struct dtrt_batch dtrt_batch;
+
+/* Build (and, with the flags, tune and capture) a batch on the current device. Tuning
+ * launches run on `stream`, which must not be capturing. */
+int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void *stream, dtrt_batch **out);
+/* Render every item; blocks until done. */
+int dtrt_batch_launch(dtrt_batch *batch, void *stream);
+int dtrt_batch_stats_get(const dtrt_batch *batch, dtrt_batch_stats *out);
+int dtrt_batch_destroy(dtrt_batch *batch);
+
 /* Closest-hit queries against the scene BVH (device kernel), for tests of the
  * traversal. rays: [n][8] = org.xyz, tmin, dir.xyz, tmax (host arrays).
  * hits: [n][2] int = (global triangle id or -1, shape id); t: [n] float. */

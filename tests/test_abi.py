@@ -31,18 +31,21 @@ def test_exports_every_declared_symbol(lib):
 def test_struct_layout_matches_c(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "dtrt_gb300.h"\nint main(void){'
-                   'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dtrt_camera_desc), '
+                   'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dtrt_camera_desc), '
                    'sizeof(dtrt_shape_desc), sizeof(dtrt_bsdf_desc), sizeof(dtrt_emitter_desc), '
                    'sizeof(dtrt_phase_desc), sizeof(dtrt_medium_desc), sizeof(dtrt_scene_desc), '
-                   'sizeof(dtrt_render_options), sizeof(dtrt_render_stats), offsetof(dtrt_medium_desc, to_world), '
-                   'offsetof(dtrt_scene_desc, edge_weights)); return 0;}\n')
+                   'sizeof(dtrt_render_options), sizeof(dtrt_render_stats), sizeof(dtrt_batch_item), '
+                   'sizeof(dtrt_batch_stats), offsetof(dtrt_medium_desc, to_world), '
+                   'offsetof(dtrt_scene_desc, edge_weights), offsetof(dtrt_batch_item, d_image), '
+                   'offsetof(dtrt_batch_stats, item_ms_estimate)); return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     want = [ctypes.sizeof(t) for t in (_abi.CameraDesc, _abi.ShapeDesc, _abi.BsdfDesc, _abi.EmitterDesc,
                                        _abi.PhaseDesc, _abi.MediumDesc, _abi.SceneDesc, _abi.RenderOptions,
-                                       _abi.RenderStats)]
-    want += [_abi.MediumDesc.to_world.offset, _abi.SceneDesc.edge_weights.offset]
+                                       _abi.RenderStats, _abi.BatchItem, _abi.BatchStats)]
+    want += [_abi.MediumDesc.to_world.offset, _abi.SceneDesc.edge_weights.offset, _abi.BatchItem.d_image.offset,
+             _abi.BatchStats.item_ms_estimate.offset]
     assert got == want
 
 

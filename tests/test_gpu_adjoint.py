@@ -182,3 +182,22 @@ def test_adjoint_device_pointers(native):
         assert np.allclose(img_d.cpu().numpy(), img_h, rtol=1e-5, atol=1e-7)
         gd = grad_d.cpu().numpy()
         assert np.abs(gd - grad_h).max() <= 1e-4 * np.abs(grad_h).max()
+
+
+def test_density_render_func_autograd(native):
+    torch = pytest.importorskip("torch")
+    from dtrt_gb300.pydtrt import DensityRenderFunc
+    res, size = 16, 24
+    spec = small_c3(nder=1, res=res, size=size)
+    with native.NativeScene(spec) as ns:
+        o = ns.options(seed=5, spp=16, max_bounces=5, sppe=0)
+        dens = torch.tensor(spec.media[0].density, requires_grad=True)
+        target = torch.zeros((size, size, 3))
+        img = DensityRenderFunc.apply(dens, ns, 0, o, 5)  # backward replays the forward seed
+        loss = ((img - target) ** 2).sum()
+        loss.backward()
+        _, g = ns.render_adjoint(2.0 * (img.detach().numpy() - target.numpy()), image=False, options=o)
+        gt = dens.grad.numpy().reshape(-1)
+        assert dens.grad.shape == dens.shape
+        assert np.abs(gt - g).max() <= 1e-4 * np.abs(g).max()
+        assert np.abs(g).max() > 0

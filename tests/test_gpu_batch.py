@@ -1,0 +1,83 @@
+"""Batches of uneven scenes in one persistent launch (dtrt_batch_*): every item's image and
+density gradient equal the single-scene adjoint render of the same options (up to the
+order of floating-point atomic adds), with and without autotuning and graph capture, and
+across repeated launches."""
+import numpy as np
+import pytest
+
+from dtrt_gb300 import _abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _items(native, torch, n=6):
+    out = []
+    for i in range(n):
+        spec, kw = scenes.config4(i, side_scale=0.125, spp_scale=0.125)
+        sc = native.NativeScene(spec)
+        h, w = spec.height, spec.width
+        opts = sc.options(seed=40 + i, spp=kw["spp"], max_bounces=kw["max_bounces"], sppe=0)
+        nvox = sc.gradient_sizes()[0]
+        dimg = torch.randn((h, w, 3), device="cuda", generator=torch.Generator("cuda").manual_seed(i))
+        img = torch.zeros((h, w, 3), device="cuda")
+        grad = torch.zeros(max(nvox, 1), device="cuda")
+        out.append(dict(scene=sc, opts=opts, dimg=dimg, img=img, grad=grad, nvox=nvox))
+    return out
+
+
+def _single(it, torch):
+    img = torch.zeros_like(it["img"])
+    grad = torch.zeros_like(it["grad"])
+    s = torch.cuda.current_stream().cuda_stream
+    it["scene"].render_adjoint(it["dimg"].data_ptr(), image=img.data_ptr(),
+                               density_grad=grad.data_ptr() if it["nvox"] else None, stream=s, device=True,
+                               options=it["opts"])
+    torch.cuda.synchronize()
+    return img.cpu().numpy(), grad.cpu().numpy()
+
+
+@pytest.mark.parametrize("autotune,graph", [(True, True), (False, False), (False, True)])
+def test_batch_matches_single_renders(native, autotune, graph):
+    torch = pytest.importorskip("torch")
+    items = _items(native, torch)
+    assert any(it["nvox"] for it in items) and any(not it["nvox"] for it in items)
+    ref = [_single(it, torch) for it in items]
+    batch = native.Batch([(it["scene"], it["opts"], it["dimg"].data_ptr(), it["img"].data_ptr(),
+                           it["grad"].data_ptr() if it["nvox"] else 0) for it in items], autotune=autotune,
+                         graph=graph, stream=torch.cuda.current_stream().cuda_stream)
+    st = batch.stats()
+    assert st["num_items"] == len(items) and st["graph"] == graph
+    if autotune:
+        assert len(st["trials"]) >= 2
+        assert sorted(st["order"]) == list(range(len(items)))
+    for rep in range(2):  # a second launch rewrites the same results
+        batch.launch(torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        for it, (img_r, grad_r) in zip(items, ref):
+            img = it["img"].cpu().numpy()
+            assert np.abs(img - img_r).max() <= 1e-5 * max(1e-3, np.abs(img_r).max())
+            assert img.sum() > 0
+            if it["nvox"]:
+                g = it["grad"].cpu().numpy()
+                assert np.abs(g - grad_r).max() <= 1e-4 * max(1e-12, np.abs(grad_r).max())
+                assert np.abs(g).max() > 0
+    batch.close()
+    for it in items:
+        it["scene"].close()
+
+
+def test_batch_rejects_bad_items(native):
+    torch = pytest.importorskip("torch")
+    lib = _abi.load()
+    h = _abi.ctypes.c_void_p()
+    arr = (_abi.BatchItem * 1)()
+    assert lib.dtrt_batch_create(arr, 0, 0, None, _abi.ctypes.byref(h)) == _abi.DTRT_ERR_INVALID
+    spec, kw = scenes.config4(1, side_scale=0.125, spp_scale=0.125)
+    with native.NativeScene(spec) as sc:
+        arr[0].scene = sc.handle.value
+        arr[0].opts = sc.options(spp=1, max_bounces=2)
+        # no output buffer
+        assert lib.dtrt_batch_create(arr, 1, 0, None, _abi.ctypes.byref(h)) == _abi.DTRT_ERR_INVALID
+        g = torch.zeros(16, device="cuda")
+        arr[0].d_density = g.data_ptr()  # d_density without d_image
+        assert lib.dtrt_batch_create(arr, 1, 0, None, _abi.ctypes.byref(h)) == _abi.DTRT_ERR_INVALID

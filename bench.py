@@ -429,7 +429,7 @@ def adjoint_throughput_c3(steps=3, warmup=1, size=512, spp=128):
             "paths_per_s": size * size * spp / (ms / 1e3), "ms_per_pass": ms}
 
 
-def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2):
+def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=1, tune_full=True):
     """C4: n seeded scenes of uneven size (1k-50k triangles, half with a 32^3-128^3 grid,
     128^2-512^2, 16-256 spp, depth 4-16), image + density gradient per scene, as one
     autotuned persistent launch replayed from a CUDA graph, against the same renders issued
@@ -467,7 +467,8 @@ def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2):
     ms_seq = e0.elapsed_time(e1) / reps
     t0 = time.perf_counter()
     batch = native.Batch([(sc, opts, dimg.data_ptr(), img.data_ptr(), grad.data_ptr() if nvox else 0)
-                          for sc, opts, dimg, img, grad, nvox in items], autotune=True, graph=True, stream=sptr)
+                          for sc, opts, dimg, img, grad, nvox in items], autotune=True, graph=True, stream=sptr,
+                         tune_full=tune_full)
     tune_s = time.perf_counter() - t0
     batch.launch(sptr)  # warm-up
     torch.cuda.synchronize()
@@ -484,8 +485,10 @@ def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2):
     return {"workload": f"C4 {n} scenes (side x{side_scale}, spp x{spp_scale}): image + density gradient",
             "paths": total_paths, "ms_one_at_a_time": ms_seq, "ms_batch": ms_batch,
             "paths_per_s_batch": total_paths / (ms_batch / 1e3), "speedup": ms_seq / ms_batch,
-            "tune_and_capture_s": tune_s, "chunk_paths": st["chunk_paths"],
+            "tune_and_capture_s": tune_s, "schedule": st["schedule"], "streams": st["streams"],
+            "chunk_paths": st["chunk_paths"],
             "order_longest_first": st["order_longest_first"], "grid_blocks": st["grid_blocks"],
+            "full_size_trials_ms": st["full_size_ms"],
             "trials": st["trials"]}
 
 

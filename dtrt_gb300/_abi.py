@@ -135,7 +135,7 @@ class RenderStats(ctypes.Structure):
 
 
 BATCH_MAX_ITEMS, BATCH_MAX_TRIALS = 256, 16
-BATCH_AUTOTUNE, BATCH_GRAPH = 1, 2
+BATCH_AUTOTUNE, BATCH_GRAPH, BATCH_TUNE_FULL = 1, 2, 4
 
 
 class BatchItem(ctypes.Structure):
@@ -146,21 +146,29 @@ class BatchItem(ctypes.Structure):
 class BatchStats(ctypes.Structure):
     _fields_ = [
         ("num_items", ctypes.c_int), ("total_paths", ctypes.c_uint64), ("grid_blocks", ctypes.c_int),
-        ("blocks_per_sm", ctypes.c_int), ("chunk_paths", ctypes.c_int), ("order_longest_first", ctypes.c_int),
+        ("blocks_per_sm", ctypes.c_int), ("schedule", ctypes.c_int), ("streams", ctypes.c_int),
+        ("chunk_paths", ctypes.c_int), ("order_longest_first", ctypes.c_int),
         ("graph", ctypes.c_int), ("num_trials", ctypes.c_int),
         ("trial_chunk", ctypes.c_int * BATCH_MAX_TRIALS), ("trial_order", ctypes.c_int * BATCH_MAX_TRIALS),
         ("trial_ms", ctypes.c_float * BATCH_MAX_TRIALS), ("tune_sample_stride", ctypes.c_int64),
+        ("full_ms", ctypes.c_float * 4),
         ("item_ms_estimate", ctypes.c_double * BATCH_MAX_ITEMS), ("order", ctypes.c_int * BATCH_MAX_ITEMS),
     ]
 
     def as_dict(self):
         n, t = self.num_items, self.num_trials
         return {"num_items": n, "total_paths": self.total_paths, "grid_blocks": self.grid_blocks,
-                "blocks_per_sm": self.blocks_per_sm, "chunk_paths": self.chunk_paths,
+                "blocks_per_sm": self.blocks_per_sm,
+                "schedule": "per_item_launches" if self.schedule == 1 else "persistent", "streams": self.streams,
+                "chunk_paths": self.chunk_paths,
                 "order_longest_first": bool(self.order_longest_first), "graph": bool(self.graph),
-                "trials": [{"chunk": self.trial_chunk[i], "order": "longest_first" if self.trial_order[i] == 0
-                            else "input", "ms": self.trial_ms[i]} for i in range(t)],
+                "trials": [{"schedule": "per_item_launches" if self.trial_chunk[i] < 0 else "persistent",
+                            "chunk": max(self.trial_chunk[i], 0), "streams": max(-self.trial_chunk[i], 1),
+                            "order": "longest_first" if self.trial_order[i] == 0 else "input",
+                            "ms": self.trial_ms[i]} for i in range(t)],
                 "tune_sample_stride": self.tune_sample_stride,
+                "full_size_ms": {"persistent": self.full_ms[0], "per_item_1": self.full_ms[1],
+                                 "per_item_2": self.full_ms[2], "per_item_4": self.full_ms[3]},
                 "item_ms_estimate": list(self.item_ms_estimate[:min(n, BATCH_MAX_ITEMS)]),
                 "order": list(self.order[:min(n, BATCH_MAX_ITEMS)])}
 
@@ -180,6 +188,8 @@ _SIGNATURES = {
                                        ctypes.c_int, ctypes.c_void_p]),
     "dtrt_render_fwd_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
                                                ctypes.c_int, ctypes.c_void_p]),
+    "dtrt_render_primal": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
+                                          ctypes.c_int, ctypes.c_void_p]),
     "dtrt_scene_enable_counters": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dtrt_scene_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderStats)]),
     "dtrt_scene_set_queue_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),

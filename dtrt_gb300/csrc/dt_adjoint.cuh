@@ -197,9 +197,10 @@ DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, 
 // FP64 [npix][3]. Contains warp collectives: all 32 lanes of a warp must call it together.
 template <int N>
 DT_D void adjoint_one(const DevScene &sc, const RenderParams &rp, int *stack, long long gi, const float *dimg,
-                      float *grad, double *img_acc, Ctr &c) {
-    const bool active = gi < rp.path_count;
-    const long long g = rp.path_begin + (active ? gi : 0);
+                      float *grad, double *img_acc, Ctr &c, long long stride = 1) {
+    // stride > 1 (autotuning samples): path gi*stride of the range
+    const bool active = gi * stride < rp.path_count;
+    const long long g = rp.path_begin + (active ? gi * stride : 0);
     const int pixel = (int)(g / rp.spp);
     AdjCtx adj{grad, 0.f};
     float3 total = mk(0.f, 0.f, 0.f);
@@ -228,10 +229,11 @@ DT_D void adjoint_one(const DevScene &sc, const RenderParams &rp, int *stack, lo
 // One thread per camera path of one scene.
 template <int N>
 __global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp, const float *dimg, float *grad,
-                                                    double *img_acc, unsigned long long *ctr) {
+                                                    double *img_acc, unsigned long long *ctr, long long stride = 1) {
     __shared__ int s_stack[kStackDepth * kBlock];
     Ctr c;
-    adjoint_one<N>(sc, rp, s_stack + threadIdx.x, (long long)blockIdx.x * kBlock + threadIdx.x, dimg, grad, img_acc, c);
+    adjoint_one<N>(sc, rp, s_stack + threadIdx.x, (long long)blockIdx.x * kBlock + threadIdx.x, dimg, grad, img_acc, c,
+                   stride);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 

@@ -601,6 +601,8 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
     // ------------------------------------------------------------ primary edges, edge_manager.cpp:6-110
     std::vector<DevPrimaryEdge> pedges;
     std::vector<double> plen;
+    std::vector<float> pjac;
+    std::vector<int> pverts;
     const double aspect = (double)c.width / c.height, fov = c2ndc[0];
     for (int si = 0; si < d->num_shapes; ++si) {
         const DevShape &sh = shapes[si];
@@ -683,6 +685,35 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
                 for (int a = 0; a < 3; ++a) dsts[q][a] = srcs[q][a];
             pedges.push_back(pe);
             plen.push_back(std::hypot(pe.v0s[0] - pe.v1s[0], pe.v0s[1] - pe.v1s[1]));
+            // Jacobian of the two clipped screen endpoints (pixels) w.r.t. the edge's vertex
+            // positions (dual slots 0-2: v0, 3-5: v1) for a static camera: the same near-plane
+            // clip, projection and image clip as above, for the vertex-position adjoint
+            {
+                const HV o0 = vad[si][e.v0 - sh.vert_off], o1 = vad[si][e.v1 - sh.vert_off];
+                HV a = {HD(o0.x.v), HD(o0.y.v), HD(o0.z.v)}, b = {HD(o1.x.v), HD(o1.y.v), HD(o1.z.v)};
+                for (int q = 0; q < 3; ++q) { a[q].d[q] = 1.0; b[q].d[3 + q] = 1.0; }
+                if (z0 < near) a = a + (b - a) * ((near - z0) / (z1 - z0));
+                else if (z1 < near) b = b + (a - b) * ((near - z1) / (z0 - z1));
+                const HV cp0 = {HD(cpos.x), HD(cpos.y), HD(cpos.z)};
+                const HV cf0[3] = {{HD(fr[0].x), HD(fr[0].y), HD(fr[0].z)}, {HD(fr[1].x), HD(fr[1].y), HD(fr[1].z)},
+                                   {HD(fr[2].x), HD(fr[2].y), HD(fr[2].z)}};
+                a = (a - cp0) / hdot(a - cp0, cf0[2]);
+                b = (b - cp0) / hdot(b - cp0, cf0[2]);
+                a = {hdot(a, cf0[0]), hdot(a, cf0[1]), hdot(a, cf0[2])};
+                b = {hdot(b, cf0[0]), hdot(b, cf0[1]), hdot(b, cf0[2])};
+                HD q0[2] = {a.x * (fov * 0.5) + HD(0.5), a.y * (fov * -0.5 * aspect) + HD(0.5)};
+                HD q1[2] = {b.x * (fov * 0.5) + HD(0.5), b.y * (fov * -0.5 * aspect) + HD(0.5)};
+                HD k0[2], k1[2];
+                const bool vis = clip_line(q0, q1, k0, k1, xmin, xmax, ymin, ymax);
+                for (int q = 0; q < 6; ++q) {
+                    pjac.push_back(vis ? (float)(k0[0].d[q] * c.width) : 0.f);
+                }
+                for (int q = 0; q < 6; ++q) pjac.push_back(vis ? (float)(k0[1].d[q] * c.height) : 0.f);
+                for (int q = 0; q < 6; ++q) pjac.push_back(vis ? (float)(k1[0].d[q] * c.width) : 0.f);
+                for (int q = 0; q < 6; ++q) pjac.push_back(vis ? (float)(k1[1].d[q] * c.height) : 0.f);
+                pverts.push_back(e.v0);
+                pverts.push_back(e.v1);
+            }
         }
     }
     std::vector<double> pcdf;
@@ -706,7 +737,8 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
         !bld.upload(light_cdf, &ds.light_cdf) || !bld.upload(light_pmf, &ds.light_pmf) ||
         !bld.upload(light_area, &ds.light_area) || !bld.upload(area_cdf, &ds.area_cdf) ||
         !bld.upload(area_begin, &ds.area_cdf_begin) || !bld.upload(edges, &ds.edges) ||
-        !bld.upload(edge_cdf, &ds.edge_cdf) || !bld.upload(pedges, &ds.pedges) || !bld.upload(pcdf, &ds.pedge_cdf))
+        !bld.upload(edge_cdf, &ds.edge_cdf) || !bld.upload(pedges, &ds.pedges) || !bld.upload(pcdf, &ds.pedge_cdf) ||
+        !bld.upload(pjac, &ds.pedge_jac) || !bld.upload(pverts, &ds.pedge_verts))
         return DTRT_ERR_CUDA;
     if (!any_normals) ds.normal_der = nullptr;
     ds.num_bsdfs = d->num_bsdfs;
@@ -979,17 +1011,20 @@ int dtrt_render_adjoint(dtrt_scene *scene, const dtrt_render_options *opts, cons
         dt::set_last_error("null argument");
         return DTRT_ERR_INVALID;
     }
+    if ((d_density || d_vertices) && !d_image) {
+        dt::set_last_error("d_density and d_vertices need d_image");
+        return DTRT_ERR_INVALID;
+    }
+    if (opts->spp < 0 || opts->sppse < 0) {
+        dt::set_last_error("spp and sppse must be >= 0");
+        return DTRT_ERR_INVALID;
+    }
     if (d_vertices) {
-        dt::set_last_error("the vertex-position adjoint is not built; use forward-mode velocities");
-        return DTRT_ERR_UNSUPPORTED;
-    }
-    if (d_density && !d_image) {
-        dt::set_last_error("d_density needs d_image");
-        return DTRT_ERR_INVALID;
-    }
-    if (opts->spp < 0) {
-        dt::set_last_error("spp must be >= 0");
-        return DTRT_ERR_INVALID;
+        if (d_density && scene->density_voxels > 0) {
+            dt::set_last_error("the vertex-position adjoint needs a scene without participating media");
+            return DTRT_ERR_UNSUPPORTED;
+        }
+        return dt::render_vertex_adjoint(scene, opts, d_image, image, d_vertices, on_device, (cudaStream_t)stream);
     }
     return dt::render_adjoint(scene, opts, d_image, image, d_density, on_device, (cudaStream_t)stream);
 }

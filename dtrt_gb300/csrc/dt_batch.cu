@@ -14,8 +14,10 @@
 //
 // Autotuner: (1) a probe launch per item on a sample of its paths measures the cost per
 // path; items are then ordered longest-total-cost first (or kept in input order, whichever
-// times faster); (2) the chunk size is chosen among 32..512 paths by timing the whole batch
-// on a strided sample of every item's paths.
+// times faster); (2) the schedule is timed on a strided sample of every item's paths: the
+// persistent launch with chunks of 32..512 paths, or one launch per item (scene data as
+// kernel parameters) dealt over 1, 2 or 4 streams so that one item's tail overlaps the
+// next item; the fastest is captured.
 #include <algorithm>
 #include <cstring>
 #include <memory>
@@ -40,9 +42,17 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchItemDev *items, con
                                                   int n, long long total_chunks, int chunk, long long sample_stride,
                                                   unsigned long long *next) {
     __shared__ int s_stack[kStackDepth * kBlock];
+    // the current item's scene and parameters, one copy per warp: the path code reads them
+    // at every step, and shared memory serves those uniform reads like kernel parameters do
+    __shared__ DevScene s_sc[kBlock / 32];
+    __shared__ RenderParams s_rp[kBlock / 32];
     int *stack = s_stack + threadIdx.x;
     const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int cur = -1;
+    const float *dimg = nullptr;
+    float *grad = nullptr;
+    double *img_acc = nullptr;
     for (;;) {
         unsigned long long c = 0;
         if (lane == 0) c = atomicAdd(next, 1ull);
@@ -54,14 +64,26 @@ __global__ void __launch_bounds__(kBlock) k_batch(const BatchItemDev *items, con
             if ((unsigned long long)cbeg[mid] <= c) lo = mid;
             else hi = mid - 1;
         }
-        const BatchItemDev &it = items[order[lo]];
+        const int item = order[lo];
+        if (item != cur) {  // warp-uniform: copy the item's scene and parameters into shared memory
+            __syncwarp();
+            const BatchItemDev &it = items[item];
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&it.sc);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&s_sc[warp]);
+            for (int k = lane; k < (int)(sizeof(DevScene) / 4); k += 32) dst[k] = src[k];
+            src = reinterpret_cast<const uint32_t *>(&it.rp);
+            dst = reinterpret_cast<uint32_t *>(&s_rp[warp]);
+            for (int k = lane; k < (int)(sizeof(RenderParams) / 4); k += 32) dst[k] = src[k];
+            dimg = it.dimg;
+            grad = it.grad;
+            img_acc = it.img_acc;
+            cur = item;
+            __syncwarp();
+        }
         const long long base = ((long long)c - cbeg[lo]) * chunk;
         Ctr ctr;
-        for (int k = lane; k < chunk; k += 32) {
-            // sample_stride > 1 (tuning): every stride-th path of the item, same layout
-            const long long gi = (base + k) * sample_stride;
-            adjoint_one<1>(it.sc, it.rp, stack, gi, it.dimg, it.grad, it.img_acc, ctr);
-        }
+        for (int k = lane; k < chunk; k += 32)  // sample_stride > 1 (tuning): every stride-th path
+            adjoint_one<1>(s_sc[warp], s_rp[warp], stack, base + k, dimg, grad, img_acc, ctr, sample_stride);
     }
 }
 
@@ -108,6 +130,11 @@ struct dtrt_batch {
     long long total_chunks = 0, total_pix = 0;
     std::vector<int> order;
     std::vector<long long> cbeg;
+    // schedule: 0 persistent launch, 1 one launch per item spread over `nstreams` streams
+    int schedule = 0, nstreams = 1;
+    std::vector<cudaStream_t> side;  // streams 1.. of the per-item schedule
+    std::vector<cudaEvent_t> side_ev;
+    cudaEvent_t fork_ev = nullptr;
     // graph
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -128,6 +155,9 @@ namespace {
     } while (0)
 
 void free_batch(dtrt_batch *b) {
+    for (cudaStream_t x : b->side) cudaStreamDestroy(x);
+    for (cudaEvent_t x : b->side_ev) cudaEventDestroy(x);
+    if (b->fork_ev) cudaEventDestroy(b->fork_ev);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
@@ -171,6 +201,35 @@ int launch_once(dtrt_batch *b, const std::vector<int> &order, int chunk, long lo
     DT_BCK(cudaStreamSynchronize(st));  // the layout buffers may still be read by a previous launch
     int rc = upload_layout(b, order, chunk, stride, total);
     return rc ? rc : launch_kernel(b, total, chunk, stride, st);
+}
+
+// one k_adjoint launch per item (every stride-th path), items dealt round-robin in `order`
+// to st and S-1 side streams that fork from and join back into st (graph-capturable)
+int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long stride, cudaStream_t st) {
+    S = std::max(1, std::min(S, 1 + (int)b->side.size()));
+    if (S > 1) {
+        DT_BCK(cudaEventRecord(b->fork_ev, st));
+        for (int k = 1; k < S; ++k) DT_BCK(cudaStreamWaitEvent(b->side[k - 1], b->fork_ev, 0));
+    }
+    for (size_t i = 0; i < order.size(); ++i) {
+        const BatchItemDev &it = b->host_items[order[i]];
+        const long long n = (it.rp.path_count + stride - 1) / stride;
+        if (n <= 0) continue;
+        cudaStream_t q = (i % S == 0) ? st : b->side[i % S - 1];
+        k_adjoint<1><<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, q>>>(it.sc, it.rp, it.dimg, it.grad, it.img_acc,
+                                                                              nullptr, stride);
+        DT_BCK(cudaGetLastError());
+    }
+    for (int k = 1; k < S; ++k) {
+        DT_BCK(cudaEventRecord(b->side_ev[k - 1], b->side[k - 1]));
+        DT_BCK(cudaStreamWaitEvent(st, b->side_ev[k - 1], 0));
+    }
+    return DTRT_OK;
+}
+
+int launch_schedule(dtrt_batch *b, cudaStream_t st, long long stride) {
+    if (b->schedule == 1) return launch_items(b, b->order, b->nstreams, stride, st);
+    return launch_once(b, b->order, b->chunk, stride, st);
 }
 
 int zero_outputs(dtrt_batch *b, cudaStream_t st) {
@@ -262,8 +321,71 @@ int autotune(dtrt_batch *b, cudaStream_t st) {
             }
         }
     }
+    // one launch per item over 1, 2 or 4 streams (longest first)
+    for (int S : {1, 2, 4}) {
+        float ms = 0.f;
+        DT_BCK(cudaStreamSynchronize(st));
+        int rc = timed(st, [&]() { return launch_items(b, longest, S, stride, st); }, ms);
+        if (rc) return rc;
+        if (trial < DTRT_BATCH_MAX_TRIALS) {
+            b->stats.trial_chunk[trial] = -S;  // negative: per-item launches over S streams
+            b->stats.trial_order[trial] = 0;
+            b->stats.trial_ms[trial] = ms;
+        }
+        ++trial;
+        if (ms < best) {
+            best = ms;
+            b->schedule = 1;
+            b->nstreams = S;
+            b->order = longest;
+            b->stats.order_longest_first = 1;
+        }
+    }
     b->stats.num_trials = std::min(trial, DTRT_BATCH_MAX_TRIALS);
     b->stats.tune_sample_stride = stride;
+    return DTRT_OK;
+}
+
+// Full-size confirmation (DTRT_BATCH_TUNE_FULL): a strided sample shrinks every per-item
+// launch to a few waves, which understates that schedule on large items. Time the sampled
+// winner of the persistent schedule and the per-item schedule on 1, 2 and 4 streams on the
+// whole batch once each and keep the fastest.
+int autotune_full(dtrt_batch *b, cudaStream_t st) {
+    const int saved_chunk = b->chunk;
+    const std::vector<int> saved_order = b->order;
+    std::vector<int> longest(b->n);
+    std::iota(longest.begin(), longest.end(), 0);
+    std::stable_sort(longest.begin(), longest.end(), [&](int a, int c) {
+        return b->stats.item_ms_estimate[std::min(a, DTRT_BATCH_MAX_ITEMS - 1)] >
+               b->stats.item_ms_estimate[std::min(c, DTRT_BATCH_MAX_ITEMS - 1)];
+    });
+    float best = 1e30f;
+    int best_sched = 0, best_streams = 1;
+    for (int cand = 0; cand < 4; ++cand) {
+        float ms = 0.f;
+        DT_BCK(cudaStreamSynchronize(st));
+        int rc;
+        if (cand == 0) {
+            long long total = 0;
+            rc = upload_layout(b, saved_order, saved_chunk, 1, total);
+            if (rc) return rc;
+            rc = timed(st, [&]() { return launch_kernel(b, total, saved_chunk, 1, st); }, ms);
+        } else {
+            rc = timed(st, [&]() { return launch_items(b, longest, 1 << (cand - 1), 1, st); }, ms);
+        }
+        if (rc) return rc;
+        b->stats.full_ms[cand] = ms;
+        if (ms < best) {
+            best = ms;
+            best_sched = cand == 0 ? 0 : 1;
+            best_streams = cand == 0 ? 1 : 1 << (cand - 1);
+        }
+    }
+    b->schedule = best_sched;
+    b->nstreams = best_streams;
+    b->chunk = saved_chunk;
+    b->order = best_sched == 0 ? saved_order : longest;
+    b->stats.order_longest_first = best_sched == 1 ? 1 : b->stats.order_longest_first;
     return DTRT_OK;
 }
 
@@ -276,7 +398,7 @@ int capture(dtrt_batch *b) {
     if (rc) return rc;
     DT_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     rc = zero_outputs(b, cs);
-    if (!rc) rc = launch_kernel(b, total, b->chunk, 1, cs);
+    if (!rc) rc = b->schedule == 1 ? launch_items(b, b->order, b->nstreams, 1, cs) : launch_kernel(b, total, b->chunk, 1, cs);
     if (!rc && b->n_img > 0) {
         k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, cs>>>(b->d_imgs, b->n_img, b->total_pix);
         if (cudaGetLastError() != cudaSuccess) rc = DTRT_ERR_CUDA;
@@ -397,17 +519,29 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
     DT_BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
     DT_BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBlock, 0));
     b->grid = std::max(1, sms * std::max(1, per_sm));
+    DT_BCK(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
+    for (int k = 0; k < 3; ++k) {
+        cudaStream_t x;
+        cudaEvent_t ev;
+        DT_BCK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+        b->side.push_back(x);
+        DT_BCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        b->side_ev.push_back(ev);
+    }
     b->order.resize(n);
     std::iota(b->order.begin(), b->order.end(), 0);
     b->chunk = 128;
     b->stats.grid_blocks = b->grid;
     b->stats.blocks_per_sm = per_sm;
-    if (flags & DTRT_BATCH_AUTOTUNE) {
+    if (flags & (DTRT_BATCH_AUTOTUNE | DTRT_BATCH_TUNE_FULL)) {
         int rc = autotune(b.get(), st);
+        if (!rc && (flags & DTRT_BATCH_TUNE_FULL)) rc = autotune_full(b.get(), st);
         if (rc) return rc;
         DT_BCK(cudaStreamSynchronize(st));
     }
     b->stats.chunk_paths = b->chunk;
+    b->stats.schedule = b->schedule;
+    b->stats.streams = b->schedule == 1 ? b->nstreams : 1;
     for (int i = 0; i < n && i < DTRT_BATCH_MAX_ITEMS; ++i) b->stats.order[i] = b->order[i];
     b->stats.num_items = n;
     long long tp = 0;
@@ -438,7 +572,7 @@ int dtrt_batch_launch(dtrt_batch *b, void *stream) {
         DT_BCK(cudaGraphLaunch(b->exec, st));
     } else {
         int rc = zero_outputs(b, st);
-        if (!rc) rc = launch_once(b, b->order, b->chunk, 1, st);
+        if (!rc) rc = launch_schedule(b, st, 1);
         if (rc) return rc;
         if (b->n_img > 0) {
             k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, st>>>(b->d_imgs, b->n_img, b->total_pix);

@@ -1247,11 +1247,13 @@ DT_HEAVY DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &it
 }
 
 // ------------------------------------------------------------------ non-AD path, volpathAD.cpp:50-142
+// (the same loop is VolPathTracer::radiance, volpath.cpp:10-103, whose first hit is traced
+// from the camera: on_surface = false)
 DT_D float3 li_path(const DevScene &sc, int *stack, Rng &rng, float3 o, float3 d, int max_depth, int med,
-                    bool inc_emission, Ctr &c) {
+                    bool inc_emission, Ctr &c, bool on_surface = true) {
     Its its;
     float3 ret = mk(0.f, 0.f, 0.f), thr = mk(1.f, 1.f, 1.f);
-    ray_intersect(sc, stack, o, d, true, its, c);
+    ray_intersect(sc, stack, o, d, on_surface, its, c);
     for (int depth = 0; depth <= max_depth; ++depth) {
         const int max_inter = max_depth - depth - 1;
         const float r1a = rng.next1(), r1b = rng.next1();

@@ -51,6 +51,8 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
 bool ensure_buffer(void **ptr, size_t *have, size_t need);
 int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
                    int on_device, cudaStream_t stream);
+int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image,
+                          float *d_vertices, int on_device, cudaStream_t stream);
 template <int N>
 int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream,
                      unsigned char *scratch, size_t scratch_bytes);

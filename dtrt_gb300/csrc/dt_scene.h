@@ -137,6 +137,8 @@ struct DevScene {
     int has_edges;
     // primary edges, edge_manager.cpp
     const DevPrimaryEdge *pedges;
+    const float *pedge_jac;        // [num_pedges][end][x,y][6]: screen-point Jacobian (pixels) w.r.t. (v0, v1)
+    const int *pedge_verts;        // [num_pedges][2] global vertex ids of the edge
     const double *pedge_cdf;       // num_pedges+1 entries
     int num_pedges;
     double pedge_sum;

@@ -316,20 +316,18 @@ class VolPathTracerAD(Integrator):
 
 
 class VolPathTracer(Integrator):
-    """Primal volumetric path tracer: the value part of the forward-mode estimator
-    (same expectation as volpath.cpp's radiance), written to slot 0 only."""
+    """Primal volumetric path tracer (volpath.cpp:105-140 through dtrt_render_primal):
+    writes the [H, W, 3] image at the start of `rendered_image`."""
     name = "VolPathTracer"
 
     def render(self, scene, options, rendered_image):
         spec = scene.spec
-        buf = np.zeros(spec.out_shape(), np.float32)
+        n = spec.height * spec.width * 3
         o = options._c()
-        o.sppse, o.sppe = 0, 0
         lib = _abi.load()
-        _abi.check(lib.dtrt_render_fwd(scene.native.handle, ctypes.byref(o), buf.ctypes.data_as(ctypes.c_void_p), 0, None))
-        n = buf[0].size
         dst = (ctypes.c_float * n).from_address(_addr(rendered_image))
-        ctypes.memmove(dst, buf[0].ctypes.data, n * 4)
+        _abi.check(lib.dtrt_render_primal(scene.native.handle, ctypes.byref(o), ctypes.cast(dst, ctypes.c_void_p), 0,
+                                          None))
 
 
 class DirectIntegrator(Integrator):

@@ -103,6 +103,21 @@ class NativeScene:
                                              ctypes.c_void_p(stream or 0)))
         return out
 
+    def render_primal(self, out=None, stream=None, **kw):
+        """VolPathTracer image (dtrt_render_primal) into a host float32 [H, W, 3] array
+        (allocated when None) or a device pointer given as an int."""
+        o = kw.pop("options", None) or self.options(**kw)
+        if isinstance(out, int) and not isinstance(out, bool):
+            _abi.check(self.lib.dtrt_render_primal(self.handle, ctypes.byref(o), ctypes.c_void_p(out), 1,
+                                                    ctypes.c_void_p(stream or 0)))
+            return out
+        if out is None:
+            out = np.zeros(self.spec.out_shape()[1:], np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.shape == self.spec.out_shape()[1:]
+        _abi.check(self.lib.dtrt_render_primal(self.handle, ctypes.byref(o), out.ctypes.data_as(ctypes.c_void_p), 0,
+                                                ctypes.c_void_p(stream or 0)))
+        return out
+
     def render_adjoint(self, d_image=None, image=True, density_grad=True, stream=None, device=False, **kw):
         """Reverse-mode density adjoint (dtrt_render_adjoint).
 
@@ -132,6 +147,29 @@ class NativeScene:
                                                  vp(stream or 0)))
         return img, grad
 
+    def render_vertex_adjoint(self, d_image, image=True, stream=None, device=False, vertex_grad=None, **kw):
+        """Reverse-mode vertex-position adjoint (dtrt_render_adjoint with d_vertices).
+
+        Host mode: `d_image` float32 [H, W, 3]; returns (image or None, grad [num_vertices, 3]).
+        Device mode: `d_image`, `image`, `vertex_grad` are device pointers (ints); returns None."""
+        o = kw.pop("options", None) or self.options(**kw)
+        vp = ctypes.c_void_p
+        if device:
+            def dptr(x):
+                return vp(x) if type(x) is int and x != 0 else None
+            _abi.check(self.lib.dtrt_render_adjoint(self.handle, ctypes.byref(o), dptr(d_image), dptr(image), None,
+                                                     dptr(vertex_grad), 1, vp(stream or 0)))
+            return None
+        h, w = self.spec.out_shape()[1:3]
+        img = np.zeros((h, w, 3), np.float32) if image else None
+        grad = np.zeros((self.gradient_sizes()[1], 3), np.float32)
+        dimg = np.ascontiguousarray(d_image, np.float32)
+        assert dimg.shape == (h, w, 3)
+        ptr = lambda a: a.ctypes.data_as(vp) if a is not None else None
+        _abi.check(self.lib.dtrt_render_adjoint(self.handle, ctypes.byref(o), ptr(dimg), ptr(img), None, ptr(grad), 0,
+                                                 vp(stream or 0)))
+        return img, grad
+
     def trace_closest(self, rays):
         rays = np.ascontiguousarray(rays, np.float32)
         n = rays.shape[0]
@@ -148,7 +186,7 @@ class Batch:
     items: list of (NativeScene, options, d_image_ptr, image_ptr, d_density_ptr) with
     device pointers as ints (0 = none). The scenes and buffers must outlive the batch."""
 
-    def __init__(self, items, autotune=True, graph=True, stream=None):
+    def __init__(self, items, autotune=True, graph=True, stream=None, tune_full=False):
         self.lib = _abi.load()
         self.scenes = [it[0] for it in items]  # keep the scenes alive
         arr = (_abi.BatchItem * len(items))()
@@ -158,7 +196,8 @@ class Batch:
             arr[i].d_image = dimg or None
             arr[i].image = img or None
             arr[i].d_density = dden or None
-        flags = (_abi.BATCH_AUTOTUNE if autotune else 0) | (_abi.BATCH_GRAPH if graph else 0)
+        flags = (_abi.BATCH_AUTOTUNE if autotune else 0) | (_abi.BATCH_GRAPH if graph else 0) | \
+            (_abi.BATCH_TUNE_FULL if tune_full else 0)
         h = ctypes.c_void_p()
         _abi.check(self.lib.dtrt_batch_create(arr, len(items), flags, ctypes.c_void_p(stream or 0), ctypes.byref(h)))
         self.handle = h

@@ -250,6 +250,15 @@ int dtrt_render_fwd(dtrt_scene *scene, const dtrt_render_options *opts, float *o
 int dtrt_render_fwd_noalloc(dtrt_scene *scene, const dtrt_render_options *opts, float *out,
                             int out_on_device, void *stream);
 
+/* Primal render without derivatives: float[H][W][3] (crop size when cropped). Replaces
+ * VolPathTracer::render (src/integrator/volpath.cpp:105-140, bound at src/dtrt.cpp:132-134):
+ * `spp` jittered primary rays per pixel through VolPathTracer::radiance
+ * (volpath.cpp:10-103); the pixel is written unconditionally (volpath.cpp:134-136). One
+ * thread per camera path, no dual numbers; sppe, sppse, mode and ddist_coeff are ignored
+ * as in the reference. `out` is host or device memory as in dtrt_render_fwd. */
+int dtrt_render_primal(dtrt_scene *scene, const dtrt_render_options *opts, float *out, int out_on_device,
+                       void *stream);
+
 /* Enable (1) or disable (0) device work counters for later renders of a scene. */
 int dtrt_scene_enable_counters(dtrt_scene *scene, int enable);
 
@@ -295,16 +304,20 @@ int dtrt_scene_set_density(dtrt_scene *scene, int medium_id, const float *densit
 int dtrt_scene_set_density_derivatives(dtrt_scene *scene, int medium_id, const float *grids);
 
 /* Reverse-mode adjoint by path replay: the gradient of sum(d_image * I) with respect to
- * every density voxel, where I is the expected image of dtrt_render_fwd slot 0 for these
- * options. Each camera path is traced twice from its RNG seed (value, then replay with
- * scattering); nothing is stored per path. The estimate is the exact transpose of the
- * forward-mode per-voxel derivative of the same paths: projecting d_density on a direction
- * grid equals sum(d_image * derivative image) of dtrt_render_fwd with that direction set by
- * dtrt_scene_set_density_derivatives, for the same seed, up to rounding.
- *   d_image    [H][W][3] dL/dI (crop size when cropped); required with d_density
+ * every density voxel (d_density) or every vertex position (d_vertices), where I is the
+ * expected image of dtrt_render_fwd slot 0 for these options. Camera paths are replayed
+ * from their RNG seeds; nothing is stored per path. The estimate is the exact transpose of
+ * the forward-mode derivative of the same paths: projecting the gradient on a direction
+ * equals sum(d_image * derivative image) of dtrt_render_fwd with that direction set as a
+ * derivative slot (dtrt_scene_set_density_derivatives, or shape vertex velocities), for the
+ * same seed, up to rounding.
+ *   d_image    [H][W][3] dL/dI (crop size when cropped); required with a gradient output
  *   image      NULL or out [H][W][3]: the image of the same paths
  *   d_density  NULL or out [density_voxels] (dtrt_scene_gradient_sizes), overwritten
- *   d_vertices must be NULL (vertex-position adjoint: DTRT_ERR_UNSUPPORTED)
+ *   d_vertices NULL or out [vertices][3] (global vertex order: shapes in order), overwritten.
+ *              Covers the interior term (BSDF frames), secondary edges (sppse) and primary
+ *              edges (sppe) of scenes without media, vertex normals or AreaLightEx emitters
+ *              (else DTRT_ERR_UNSUPPORTED); max_bounces < 32.
  * Pointers are host memory when on_device == 0, else device memory on `stream`. */
 int dtrt_render_adjoint(dtrt_scene *scene, const dtrt_render_options *opts, const float *d_image, float *image,
                         float *d_density, float *d_vertices, int on_device, void *stream);
@@ -328,6 +341,7 @@ typedef struct {
 
 #define DTRT_BATCH_AUTOTUNE 1u /* measure item costs and pick item order and chunk size */
 #define DTRT_BATCH_GRAPH 2u    /* capture the launch in a CUDA graph */
+#define DTRT_BATCH_TUNE_FULL 4u /* also time the candidate schedules once each on the whole batch */
 #define DTRT_BATCH_MAX_ITEMS 256
 #define DTRT_BATCH_MAX_TRIALS 16
 
@@ -335,13 +349,17 @@ typedef struct {
     int num_items;
     uint64_t total_paths;
     int grid_blocks, blocks_per_sm; /* persistent grid: resident blocks only */
-    int chunk_paths;                /* paths a warp takes per counter increment */
+    int schedule;                   /* 0: persistent launch, 1: one launch per item */
+    int streams;                    /* streams of the per-item schedule */
+    int chunk_paths;                /* paths a warp takes per counter increment (schedule 0) */
     int order_longest_first;        /* 1: items ordered by measured cost, longest first */
     int graph;                      /* 1: launches replay a CUDA graph */
     int num_trials;
     int trial_chunk[DTRT_BATCH_MAX_TRIALS], trial_order[DTRT_BATCH_MAX_TRIALS];
-    float trial_ms[DTRT_BATCH_MAX_TRIALS]; /* tuning launches on a strided path sample */
+    float trial_ms[DTRT_BATCH_MAX_TRIALS]; /* tuning launches on a strided path sample;
+                                              trial_chunk < 0: per-item schedule on -chunk streams */
     int64_t tune_sample_stride;
+    float full_ms[4];               /* DTRT_BATCH_TUNE_FULL: persistent, per-item on 1, 2, 4 streams */
     double item_ms_estimate[DTRT_BATCH_MAX_ITEMS]; /* measured cost of each item (probe) */
     int order[DTRT_BATCH_MAX_ITEMS];
 } dtrt_batch_stats;

@@ -37,6 +37,10 @@ int oracle_render(const dtrt_scene_desc *desc, const dtrt_render_options *opts, 
 int oracle_render_ext(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads,
                       unsigned est_flags, const float *const *density_dirs);
 
+/* VolPathTracer::render (src/integrator/volpath.cpp:105-140): the primal image
+ * out[H][W][3] (no derivatives), written unconditionally. */
+int oracle_render_primal(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads);
+
 /* Render only the primary-edge pass (integratorAD.cpp:100-165) with a caller-chosen
  * sample count, into out[nder][H][W][3] (added to). */
 int oracle_render_primary_edges(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out,

@@ -34,6 +34,7 @@ def lib():
         L.oracle_render.argtypes = [SD, RO, fp, ctypes.c_int]
         L.oracle_render_primary_edges.argtypes = [SD, RO, fp, ctypes.c_int]
         L.oracle_render_ext.argtypes = [SD, RO, fp, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(fp)]
+        L.oracle_render_primal.argtypes = [SD, RO, fp, ctypes.c_int]
         L.oracle_pcg32.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
         L.oracle_pcg32.restype = None
         L.oracle_next1d.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, dp]
@@ -85,6 +86,18 @@ def render_ext(spec, seed=0, spp=4, max_bounces=5, sppe=0, sppse=10, mode=-1, dd
                                 arr if density_dirs else None)
     if r:
         raise RuntimeError("oracle_render_ext: " + lib().oracle_last_error().decode())
+    return out
+
+
+def render_primal(spec, seed=0, spp=4, max_bounces=5, nthreads=0):
+    """VolPathTracer image float32[H, W, 3] from the FP64 CPU oracle."""
+    desc, keep = spec.to_desc()
+    out = np.zeros(spec.out_shape()[1:], np.float32)
+    o = _opts(seed, spp, max_bounces, 0, 0)
+    r = lib().oracle_render_primal(ctypes.byref(desc), ctypes.byref(o),
+                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), nthreads)
+    if r:
+        raise RuntimeError("oracle_render_primal: " + lib().oracle_last_error().decode())
     return out
 
 

@@ -587,12 +587,14 @@ struct Integrator {
     explicit Integrator(const Scene<N> &s, int se, double dd) : sc(s), sppse(se), ddist(dd) {}
 
     // volpathAD.cpp:50-142
-    V3 li(Rng &rng, const Ray &ray_in, int max_depth, int init_med, bool inc_emission = true) const {
+    // (also VolPathTracer::radiance, volpath.cpp:10-103, with on_surface = false)
+    V3 li(Rng &rng, const Ray &ray_in, int max_depth, int init_med, bool inc_emission = true,
+          bool on_surface = true) const {
         Ray ray = ray_in;
         int med = init_med;
         Its its;
         V3 ret, thr(1, 1, 1);
-        sc.ray_intersect(ray, true, its);
+        sc.ray_intersect(ray, on_surface, its);
         for (int depth = 0; depth <= max_depth; ++depth) {
             int max_inter = max_depth - depth - 1;
             double r1[2] = {rng.next1(), rng.next1()};
@@ -1076,6 +1078,41 @@ int render_impl(const dtrt_scene_desc &d, const dtrt_render_options &o, float *o
     return 0;
 }
 
+// VolPathTracer::render (volpath.cpp:105-140): per pixel RndSampler(seed, pixel), spp
+// jittered primary rays, radiance() averaged and written unconditionally
+template <int N>
+int render_primal_impl(const dtrt_scene_desc &d, const dtrt_render_options &o, float *out, int nthreads) {
+    using namespace orc;
+    auto sc = std::make_unique<Scene<N>>();
+    std::string err = sc->build(d);
+    if (!err.empty()) {
+        g_err = err;
+        return 1;
+    }
+    Integrator<N> in(*sc, 0, 0.0);
+    const Camera<N> &cam = sc->cam;
+    const bool cropped = cam.cropped();
+    const int npix = cropped ? cam.crop_w * cam.crop_h : cam.width * cam.height;
+    const int width = cropped ? cam.crop_w : cam.width;
+    if (nthreads <= 0) nthreads = omp_get_num_procs();
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 4)
+    for (int pix = 0; pix < npix; ++pix) {
+        int ix = cropped ? cam.crop_x + pix % width : pix % width;
+        int iy = cropped ? cam.crop_y + pix / width : pix / width;
+        Rng rng(o.seed, (uint64_t)pix);
+        V3 acc;
+        for (int s = 0; s < o.spp; ++s) {
+            double jx = rng.next1(), jy = rng.next1();
+            acc += in.li(rng, cam.sample_primary_ray(ix + jx, iy + jy), o.max_bounces, cam.med_id, true, false);
+        }
+        if (o.spp > 0) acc = acc / (double)o.spp;
+        out[pix * 3 + 0] = (float)acc.x;
+        out[pix * 3 + 1] = (float)acc.y;
+        out[pix * 3 + 2] = (float)acc.z;
+    }
+    return 0;
+}
+
 template <class F>
 int dispatch(int nder, F &&f) {
     switch (nder) {
@@ -1102,6 +1139,11 @@ int oracle_render_ext(const dtrt_scene_desc *desc, const dtrt_render_options *op
     return dispatch(desc->nder, [&](auto n) {
         return render_impl<decltype(n)::value>(*desc, *opts, out, nthreads, true, true, est_flags, density_dirs);
     });
+}
+
+int oracle_render_primal(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads) {
+    if (!desc || !opts || !out) { g_err = "null argument"; return 1; }
+    return dispatch(desc->nder, [&](auto n) { return render_primal_impl<decltype(n)::value>(*desc, *opts, out, nthreads); });
 }
 
 int oracle_render_primary_edges(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads) {

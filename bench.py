@@ -280,6 +280,9 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     if rank == 0 and not args.no_grad_rmse:
         line["adjoint"] = adjoint_throughput_c3()
         line["grad_rmse"] = grad_rmse_c3(size=args.grad_size)
+        line["grad_rmse_c2"] = grad_rmse_c2()
+    if rank == 0 and not args.no_batch:
+        line["batch_c4"] = batch_c4()
     scene.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -402,6 +405,89 @@ def grad_rmse_c3(size=None, runs=16, run_spp=64, ladder_max=64, seed=31):
     return result
 
 
+def grad_rmse_c2(size=None, runs=16, run_spp=16, ladder_max=16):
+    """Time to 1% gradient RMSE on the mesh workload (C2: 20480-triangle diffuse icosphere,
+    256x256, depth 4, sppse 10, primary-edge samples 16 per spp): the vertex-position adjoint
+    (one replay gives all 30,726 vertex coordinates) against forward mode (8 seeded unit
+    vertex directions per nder-8 pass). L2 image loss against the target with every vertex
+    displaced along its normal by N(0, 0.01^2). Quantities: the gradient along the 8
+    directions (1 forward pass or 1 adjoint pass). As for C3, both methods give the same
+    estimate for the same seed, the spp to 1% relative RMSE comes from `runs` independent
+    adjoint runs, and each method's time is that spp times its measured time per spp."""
+    import torch
+    from dtrt_gb300 import native, scenes
+    W = H = size or 256
+    spec = scenes.config2(W, H, nder=8)
+    tgt = scenes.config2(W, H, nder=8, displaced=True)
+    nv = spec.shapes[0].vertices.shape[0]
+    V = torch.from_numpy(np.asarray(spec.shapes[0].velocities, np.float64).reshape(8, nv, 3)).cuda()
+    kw = lambda spp: dict(max_bounces=4, sppse=10, sppe=16 * spp)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    with native.NativeScene(tgt) as nt:
+        T = nt.render_adjoint(None, image=True, density_grad=False, seed=2, spp=256, max_bounces=4)[0]
+    sc = native.NativeScene(spec)
+    I = sc.render_adjoint(None, image=True, density_grad=False, seed=1, spp=256, max_bounces=4)[0]
+    dimg = torch.from_numpy(2.0 * (I - T) / I.size).cuda()
+    nvt = sc.gradient_sizes()[1]
+    out = torch.empty(spec.out_shape(), dtype=torch.float32, device="cuda")
+    grad = torch.empty((nvt, 3), dtype=torch.float32, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def forward_mode(spp, sd):
+        e0.record(stream)
+        sc.render(out.data_ptr(), stream=sptr, seed=sd, spp=spp, **kw(spp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return (dimg[None] * out[1:]).double().sum(dim=(1, 2, 3)).cpu().numpy(), e0.elapsed_time(e1)
+
+    def adjoint(spp, sd):
+        e0.record(stream)
+        sc.render_vertex_adjoint(dimg.data_ptr(), image=None, vertex_grad=grad.data_ptr(), stream=sptr, device=True,
+                                 seed=sd, spp=spp, **kw(spp))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return (V * grad[:nv].double()[None]).sum(dim=(1, 2)).cpu().numpy(), e0.elapsed_time(e1)
+
+    t0 = time.perf_counter()
+    G = np.stack([adjoint(run_spp, 30000 + r)[0] for r in range(runs)])
+    g_hat = G.mean(0)
+    gn2 = float(g_hat @ g_hat)
+
+    def spp_1pct(Gs):
+        m = Gs.mean(0)
+        return run_spp * float(Gs.var(0, ddof=1).sum()) / (1e-4 * float(m @ m))
+
+    s1 = spp_1pct(G)
+    brng = np.random.default_rng(0)
+    boots = sorted(spp_1pct(G[brng.integers(0, runs, runs)]) for _ in range(200))
+    result = {"workload": f"C2 {W}x{H}, 20480-triangle diffuse icosphere, depth 4, L2 loss vs normal-displaced "
+                          "target (N(0, 0.01^2))",
+              "quantities": "derivatives along 8 seeded unit vertex directions",
+              "variance_runs": {"runs": runs, "spp": run_spp, "seconds": time.perf_counter() - t0,
+                                "rel_se_of_mean": float(np.sqrt(G.var(0, ddof=1).sum() / runs / gn2))},
+              "spp_to_1pct": s1, "spp_to_1pct_bootstrap_90": [boots[10], boots[189]], "threshold": 0.01}
+    ladders = {}
+    for name, fn in (("adjoint", adjoint), ("forward_mode", forward_mode)):
+        ladder, spp = [], 1
+        while spp <= ladder_max:
+            v, ms = fn(spp, 20000 + spp)
+            ladders.setdefault(spp, []).append(v)
+            ladder.append({"spp": spp, "ms": ms, "rel_err_vs_mean": float(np.linalg.norm(v - g_hat) / np.sqrt(gn2))})
+            spp *= 2
+        ms_per_spp = ladder[-1]["ms"] / ladder[-1]["spp"]
+        result[name] = {"ladder": ladder, "ms_per_spp": ms_per_spp, "ms_to_1pct": s1 * ms_per_spp}
+    result["max_rel_diff_adjoint_vs_forward"] = max(float(np.linalg.norm(a - b) / np.sqrt(gn2))
+                                                    for a, b in ladders.values())
+    a, f = result["adjoint"], result["forward_mode"]
+    result["speedup_time_to_1pct"] = f["ms_to_1pct"] / a["ms_to_1pct"]
+    # all 30,726 vertex coordinates by forward mode: one nder-8 pass per 8 directions
+    result["forward_mode_full_gradient_s_estimate"] = f["ms_to_1pct"] * (3 * nv / 8) / 1e3
+    result["speedup_full_gradient_estimate"] = f["ms_to_1pct"] * (3 * nv / 8) / a["ms_to_1pct"]
+    sc.close()
+    return result
+
+
 def adjoint_throughput_c3(steps=3, warmup=1, size=512, spp=128):
     """Paths/s of the density adjoint (both replay passes) on the C3 workload (512x512,
     128 spp, depth 16, 128^3 grid), device-resident dL/dI and gradient."""
@@ -519,6 +605,7 @@ def main():
     ap.add_argument("--no-grad-rmse", action="store_true", help="skip the adjoint vs forward-mode gradient leg")
     ap.add_argument("--grad-size", type=int, default=None, help="image side of the gradient leg (default 512)")
     ap.add_argument("--adjoint-only", action="store_true", help="time only the C3 density adjoint replay")
+    ap.add_argument("--no-batch", action="store_true", help="skip the C4 batch leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

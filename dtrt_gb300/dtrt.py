@@ -346,9 +346,37 @@ class VolPathTracerSimple(Integrator):
     name = "VolPathTracerSimple"
 
 
-class DirectAD(Integrator):
+def _require_surface_scene(scene, name):
+    if scene.spec.media:
+        raise NotImplementedError(f"{name} ignores participating media in the reference; dtrt_gb300 renders it "
+                                  "for surface scenes only (use VolPathTracerAD)")
+
+
+class PathTracerAD(VolPathTracerAD):
+    """Surface forward-mode path tracer (pathAD.cpp) as the surface specialisation of the
+    volumetric estimator: for scenes without media both estimate the same image and
+    derivatives (interior term, edge-sampled boundary term, primary edges). The reference's
+    variant differs in random-number use and in tracing visibility instead of
+    transmittance, which changes the noise, not the expectation."""
+    name = "PathTracerAD"
+
+    def render(self, scene, options, rendered_image):
+        _require_surface_scene(scene, self.name)
+        super().render(scene, options, rendered_image)
+
+
+class DirectAD(VolPathTracerAD):
+    """Direct-illumination forward mode (directAD.cpp): emission at the camera hit, light
+    sampling and BSDF sampling of the emitters, and the edge term of the camera hit, i.e. the
+    volumetric estimator with one bounce on a surface scene. The reference weighs its two
+    light strategies with the balance heuristic instead of the power heuristic: a different
+    noise, the same expectation."""
     name = "DirectAD"
 
-
-class PathTracerAD(Integrator):
-    name = "PathTracerAD"
+    def render(self, scene, options, rendered_image):
+        _require_surface_scene(scene, self.name)
+        o = options._c()
+        o.max_bounces = 1
+        lib = _abi.load()
+        _abi.check(lib.dtrt_render_fwd(scene.native.handle, ctypes.byref(o), ctypes.c_void_p(_addr(rendered_image)),
+                                       0, None))

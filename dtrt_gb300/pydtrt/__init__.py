@@ -6,7 +6,7 @@ Use `dtrt_gb300.install_reference_names()` to make `import dtrt` / `import pydtr
 resolve to these modules for unmodified reference scripts.
 """
 from .. import dtrt as _dtrt
-from .auto_grad import ADLossFunc, DensityRenderFunc, downsample
+from .auto_grad import ADLossFunc, DensityRenderFunc, VertexRenderFunc, downsample
 from .loaders import imread, imwrite, load_mitsuba, load_obj
 from .scene_manager import SceneManager, SceneTransform
 from .scene_objects import (AreaLight, AreaLightEx, BSDF_diffuse, BSDF_null, BSDF_Phong, BSDF_roughdielectric,

@@ -114,3 +114,54 @@ class DensityRenderFunc(torch.autograd.Function):
             n *= s
         gd = torch.from_numpy(grad[ctx.offset:ctx.offset + n].reshape(tuple(ctx.shape))).to(ctx.device)
         return gd, None, None, None, None
+
+
+class VertexRenderFunc(torch.autograd.Function):
+    """The image of a surface scene as a differentiable function of all vertex positions
+    (no counterpart in the reference).
+
+    forward(vertices, spec, options, backward_seed=None) -> image [H, W, 3]
+        vertices: [total vertices, 3] in global order (the spec's shapes in order); builds
+        the device scene with them (a new BVH, as the reference rebuilds per render) and
+        renders the image of `options`;
+    backward(dL/dimage) -> dL/dvertices
+        the vertex-position adjoint (dtrt_render_adjoint with d_vertices): interior BSDF
+        frames, secondary edges (options.sppse) and primary edges (options.sppe), replayed
+        with `backward_seed` (default options.seed + 1).
+
+    `spec` is a dtrt_gb300.scenes.SceneSpec of a surface scene (no media, no vertex normals,
+    AreaLight emitters).
+    """
+
+    @staticmethod
+    def forward(ctx, vertices, spec, options, backward_seed=None):
+        import copy
+        import numpy as np
+        from .. import _abi
+        from ..native import NativeScene
+        v = vertices.detach().to("cpu", torch.float32).contiguous().numpy()
+        s2 = copy.copy(spec)
+        s2.shapes = []
+        off = 0
+        for sh in spec.shapes:
+            nv = sh.vertices.shape[0]
+            sh2 = copy.copy(sh)
+            sh2.vertices = np.ascontiguousarray(v[off:off + nv])
+            s2.shapes.append(sh2)
+            off += nv
+        if off != v.shape[0]:
+            raise ValueError(f"expected {off} vertices, got {v.shape[0]}")
+        scene = NativeScene(s2)
+        img, _ = scene.render_adjoint(None, image=True, density_grad=False, options=options)
+        o = options
+        seed = o.seed + 1 if backward_seed is None else backward_seed
+        ctx.bwd_options = _abi.RenderOptions(seed, o.spp, o.max_bounces, o.sppe, o.sppse, o.quiet, o.mode, o.ddist_coeff)
+        ctx.scene, ctx.device = scene, vertices.device
+        return torch.from_numpy(img).to(vertices.device)
+
+    @staticmethod
+    def backward(ctx, grad_image):
+        g = grad_image.detach().to("cpu", torch.float32).contiguous().numpy()
+        _, gv = ctx.scene.render_vertex_adjoint(g, image=False, options=ctx.bwd_options)
+        ctx.scene.close()
+        return torch.from_numpy(gv).to(ctx.device), None, None, None

@@ -106,3 +106,19 @@ def test_vertex_adjoint_rejects_uncovered_scenes(native):
         with pytest.raises(_abi.DtrtError) as ei:
             ns.render_vertex_adjoint(np.ones((16, 16, 3), np.float32), seed=1, spp=1, max_bounces=2)
         assert ei.value.status == _abi.DTRT_ERR_UNSUPPORTED
+
+
+def test_vertex_render_func_autograd(native):
+    torch = pytest.importorskip("torch")
+    from dtrt_gb300.pydtrt import VertexRenderFunc
+    spec = c2_small(nder=1, size=24)
+    verts = torch.tensor(np.concatenate([s.vertices for s in spec.shapes]), requires_grad=True)
+    with native.NativeScene(spec) as ns:
+        o = ns.options(seed=5, spp=8, max_bounces=3, sppse=4, sppe=32)
+        img = VertexRenderFunc.apply(verts, spec, o, 5)  # backward replays the forward seed
+        target = torch.zeros_like(img)
+        ((img - target) ** 2).sum().backward()
+        _, g = ns.render_vertex_adjoint(2.0 * (img.detach().numpy() - target.numpy()), image=False, options=o)
+    assert verts.grad.shape == verts.shape
+    assert np.abs(verts.grad.numpy() - g).max() <= 1e-4 * np.abs(g).max()
+    assert np.abs(g).max() > 0

@@ -491,6 +491,8 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
             if (bd.d_alpha) o.d_alpha[j] = bd.d_alpha[j];
             if (bd.d_eta) o.d_eta[j] = bd.d_eta[j];
             o.d_inv_eta[j] = -o.d_eta[j] / (o.eta * o.eta);
+            for (int a = 0; a < 3; ++a) o.has_der |= (o.d_diffuse[j][a] != 0.f) | (o.d_specular[j][a] != 0.f);
+            o.has_der |= (o.d_exponent[j] != 0.f) | (o.d_alpha[j] != 0.f) | (o.d_eta[j] != 0.f);
         }
     }
     std::vector<DevPhase> phases(d->num_phases);
@@ -499,7 +501,10 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
         phases[p].type = d->phases[p].type;
         phases[p].g = d->phases[p].g;
         if (d->phases[p].d_g)
-            for (int j = 0; j < N; ++j) phases[p].d_g[j] = d->phases[p].d_g[j];
+            for (int j = 0; j < N; ++j) {
+                phases[p].d_g[j] = d->phases[p].d_g[j];
+                phases[p].has_der |= phases[p].d_g[j] != 0.f;
+            }
     }
     std::vector<DevEmitter> ems(d->num_emitters);
     for (int e = 0; e < d->num_emitters; ++e) {

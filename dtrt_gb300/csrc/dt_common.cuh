@@ -201,6 +201,12 @@ struct FrameAD {
     DV<N> s, t, n;
     DT_D FrameAD() {}
     DT_D explicit FrameAD(const DV<N> &nn) : n(nn) {
+        if (nn.der_zero(0.f)) {  // a fixed normal: the plain frame, lifted
+            const Frame f(nn.val());
+            s = DV<N>(f.s);
+            t = DV<N>(f.t);
+            return;
+        }
         const float R[9] = DT_PREROT_INIT;
         DV<N> q(R[0] * nn.x + R[1] * nn.y + R[2] * nn.z, R[3] * nn.x + R[4] * nn.y + R[5] * nn.z,
                 R[6] * nn.x + R[7] * nn.y + R[8] * nn.z);

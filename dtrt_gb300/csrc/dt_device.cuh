@@ -214,6 +214,34 @@ struct RayAD {
 // utils.cpp:237-254 and shape.cpp:210-252
 template <int N>
 DT_HEAVY void shape_intersect_ad(const DevScene &sc, int prim, const RayAD<N> &ray, ItsAD<N> &its) {
+    if (!sc.vert_der && !sc.face_n_der && !sc.normal_der && ray.o.der_zero(0.f) && ray.d.der_zero(0.f)) {
+        // static geometry hit by a ray without derivatives: every slot is zero; the values
+        // below follow the dual expressions operation for operation
+        const int4 tri = __ldg(sc.tris + prim);
+        const float3 o = ray.o.val(), d = ray.d.val();
+        const float3 v0 = f3(__ldg(sc.verts + tri.x)), e1 = f3(__ldg(sc.verts + tri.y)) - v0,
+                     e2 = f3(__ldg(sc.verts + tri.z)) - v0, pv = cross(d, e2);
+        float div = dot(pv, e1);
+        if (fabsf(div) < kEps) div = div > 0.f ? kEps : -kEps;
+        const float3 s = o - v0, q = cross(s, e1);
+        const float idiv = 1.0f / div;
+        const float u = dot(s, pv) * idiv, v = dot(d, q) * idiv, t = dot(e2, q) * idiv, w = 1.f - (u + v);
+        float3 gn = f3(__ldg(sc.face_n + prim)), sn = gn;
+        const DevShape &sh = sc.shapes[tri.w];
+        if (sh.has_normals) {
+            sn = normalize(f3(__ldg(sc.normals + tri.x)) * w + f3(__ldg(sc.normals + tri.y)) * u +
+                           f3(__ldg(sc.normals + tri.z)) * v);
+            if (dot(gn, sn) < 0.f) gn = -gn;
+        }
+        its.shape = tri.w;
+        its.prim = prim;
+        its.t = Df<N>(t);
+        its.p = DV<N>(o + d * t);
+        its.ng = gn;
+        its.ns = DV<N>(sn);
+        its.wi = DV<N>(Frame(sn).to_local(-d));
+        return;
+    }
     const int4 tri = __ldg(sc.tris + prim);
     const DV<N> v0 = vertex_ad<N>(sc, tri.x), v1 = vertex_ad<N>(sc, tri.y), v2 = vertex_ad<N>(sc, tri.z);
     const DV<N> e1 = v1 - v0, e2 = v2 - v0, pv = cross(ray.d, e2);
@@ -436,6 +464,8 @@ DT_D float3 bsdf_eval(const DevBsdf &b, float3 wi, float3 wo) {
 
 template <int N>
 DT_D DV<N> bsdf_eval_ad(const DevBsdf &b, const DV<N> &wi, const DV<N> &wo) {
+    // no parameter slots and fixed directions: the plain evaluation, lifted (all slots zero)
+    if (!b.has_der && wi.der_zero(0.f) && wo.der_zero(0.f)) return DV<N>(bsdf_eval(b, wi.val(), wo.val()));
     switch (b.type) {
         case BSDF_NULL: return DV<N>(mk(1.f, 1.f, 1.f));
         case BSDF_DIFFUSE:  // diffuse.cpp:15-20
@@ -565,10 +595,17 @@ DT_D DV<N> bsdf_sample_ad(const DevBsdf &b, const ItsAD<N> &its, const FrameAD<N
     }
     float3 wo0;
     DV<N> ret;
+    const bool fixed = !b.has_der && its.wi.der_zero(0.f) && fr.n.der_zero(0.f);
     if (!is_zero3(bsdf_sample(b, its0.wi, r0, r1, r2, wo0, pdf, eta)))
         if (pdf > kEps) {
-            wo = fr.to_local(its0.to_world(wo0));
-            ret = bsdf_eval_ad<N>(b, its.wi, wo) / pdf;
+            if (fixed) {  // no slot can become non-zero: plain evaluation, lifted
+                const float3 w = fr.plain().to_local(its0.to_world(wo0));
+                wo = DV<N>(w);
+                ret = DV<N>(bsdf_eval(b, its.wi.val(), w) / pdf);
+            } else {
+                wo = fr.to_local(its0.to_world(wo0));
+                ret = bsdf_eval_ad<N>(b, its.wi, wo) / pdf;
+            }
         }
     return ret;
 }
@@ -582,6 +619,7 @@ DT_D float phase_eval(const DevPhase &p, float3 wi, float3 wo) {
 template <int N>
 DT_D Df<N> phase_eval_ad(const DevPhase &p, const DV<N> &wi, const DV<N> &wo) {
     if (p.type == PHASE_ISOTROPIC) return Df<N>(kInvFourPi);
+    if (!p.has_der && wi.der_zero(0.f) && wo.der_zero(0.f)) return Df<N>(phase_eval(p, wi.val(), wo.val()));
     Df<N> g = load_dual<N>(p.g, p.d_g);
     Df<N> tmp = 1.f + g * g + 2.f * g * dot(wi, wo);
     return kInvFourPi * (1.f - g * g) / dpow(tmp, 1.5f);

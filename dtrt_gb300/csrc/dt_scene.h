@@ -37,12 +37,14 @@ struct DevBsdf {
     float diffuse[3], specular[3], exponent, alpha, eta, inv_eta, spec_weight;
     float d_diffuse[kMaxNder][3], d_specular[kMaxNder][3], d_exponent[kMaxNder];
     float d_alpha[kMaxNder], d_eta[kMaxNder], d_inv_eta[kMaxNder];
+    int has_der;  // any non-zero derivative slot (else the plain evaluation is exact)
 };
 
 struct DevPhase {
     int type;
     float g;
     float d_g[kMaxNder];
+    int has_der;  // any non-zero derivative slot
 };
 
 struct DevEmitter {

@@ -137,7 +137,7 @@ def test_adjoint_arguments_and_updates(native):
     o = ns.options(**kw)
     g = np.zeros(res ** 3, np.float32)
     vp = _abi.ctypes.c_void_p
-    # vertex adjoint is not built; d_density needs d_image; homogeneous medium ids are rejected
+    # a grid-medium scene has no vertex adjoint; d_density needs d_image; homogeneous medium ids are rejected
     assert lib.dtrt_render_adjoint(h, _abi.ctypes.byref(o), zero.ctypes.data_as(vp), None, g.ctypes.data_as(vp),
                                    g.ctypes.data_as(vp), 0, None) == _abi.DTRT_ERR_UNSUPPORTED
     assert lib.dtrt_render_adjoint(h, _abi.ctypes.byref(o), None, None, g.ctypes.data_as(vp), None, 0,

@@ -921,6 +921,20 @@ DT_HEAVY void int_sig_t(const DevScene &sc, const DevMedium &m, const RayAD<N> &
     for (int j = 0; j < N; ++j) out[j] = 0.f;
     const float len = tmax.v - tmin.v;
     const bool scatter = adj != nullptr && m.grad_off >= 0 && adj->w != 0.f;
+    if (scale.der_zero(0.f) && !m.density.moving && !(m.density.dgrid && m.density.dgrid_n == N) &&
+        ray.o.der_zero(0.f) && ray.d.der_zero(0.f) && tmin.der_zero(1e-6f) && tmax.der_zero(1e-6f)) {
+        // nothing in the integral carries a derivative: every slot is zero. Draw the same
+        // random numbers; the scatter pass only needs the sample positions.
+        const float3 o = ray.o.val(), d = ray.d.val();
+        for (int i = 0; i < 10; ++i) {
+            const float r = ((float)i + rng.next1()) * 0.1f;
+            if (scatter) {
+                const float tt = tmin.v + len * r;
+                grid_scatter(m.density, adj->grad + m.grad_off, o + d * tt, -adj->w * m.scale * len * 0.1f);
+            }
+        }
+        return;
+    }
     for (int i = 0; i < 10; ++i) {
         const float r = ((float)i + rng.next1()) * 0.1f;
         const Df<N> tt = tmin + len * r;

@@ -129,6 +129,23 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
+# --------------------------------------------------------------------------- replicas
+def max_over_ranks(ms, world, device="cuda"):
+    """The slowest rank's time (ms): replicas run in parallel, the job ends with the last."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank_step, steps, world, ms_local, device="cuda"):
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    t_max = max_over_ranks(ms_local, world, device)
+    return units_per_rank_step * steps * world / (t_max / 1e3), t_max
+
+
 # --------------------------------------------------------------------------- reference arm
 def run_reference(args, wl_name, rank):
     """The reference's CPU algorithm (IntegratorAD::render + VolPathTracerAD restated in
@@ -214,12 +231,7 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = paths_per_step * args.steps * world / (t_max / 1e3)
+    value, t_max = job_throughput(paths_per_step, args.steps, world, ms, "cuda")
     # end to end through the public API with host buffers: scene upload + BVH build + render + D2H
     e2e_steps = max(1, min(args.steps, 3))
     host_out = np.zeros(spec.out_shape(), np.float32)

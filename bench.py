@@ -527,7 +527,7 @@ def adjoint_throughput_c3(steps=3, warmup=1, size=512, spp=128):
             "paths_per_s": size * size * spp / (ms / 1e3), "ms_per_pass": ms}
 
 
-def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=1, tune_full=True):
+def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2, tune_full=True):
     """C4: n seeded scenes of uneven size (1k-50k triangles, half with a 32^3-128^3 grid,
     128^2-512^2, 16-256 spp, depth 4-16), image + density gradient per scene, as one
     autotuned persistent launch replayed from a CUDA graph, against the same renders issued
@@ -555,27 +555,27 @@ def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=1, tune_full=True):
             sc.render_adjoint(dimg.data_ptr(), image=img.data_ptr(), density_grad=grad.data_ptr() if nvox else None,
                               stream=sptr, device=True, options=opts)
 
-    one_at_a_time()  # warm-up
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(reps):
-        one_at_a_time()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_seq = e0.elapsed_time(e1) / reps
     t0 = time.perf_counter()
     batch = native.Batch([(sc, opts, dimg.data_ptr(), img.data_ptr(), grad.data_ptr() if nvox else 0)
                           for sc, opts, dimg, img, grad, nvox in items], autotune=True, graph=True, stream=sptr,
                          tune_full=tune_full)
     tune_s = time.perf_counter() - t0
+    one_at_a_time()  # warm-up
     batch.launch(sptr)  # warm-up
     torch.cuda.synchronize()
-    e0.record(stream)
+    # interleaved repetitions: both schedules run under the same clocks and power state
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    t_seq, t_batch = [], []
     for _ in range(reps):
-        batch.launch(sptr)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms_batch = e0.elapsed_time(e1) / reps
+        for fn, acc in ((one_at_a_time, t_seq), (lambda: batch.launch(sptr), t_batch)):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            acc.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    ms_seq, ms_batch = float(np.median(t_seq)), float(np.median(t_batch))
     st = batch.stats()
     batch.close()
     for it in items:
@@ -586,8 +586,8 @@ def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=1, tune_full=True):
             "tune_and_capture_s": tune_s, "schedule": st["schedule"], "streams": st["streams"],
             "chunk_paths": st["chunk_paths"],
             "order_longest_first": st["order_longest_first"], "grid_blocks": st["grid_blocks"],
-            "full_size_trials_ms": st["full_size_ms"],
-            "trials": st["trials"]}
+            "full_size_trials_ms": st["full_size_ms"], "reps_ms": {"one_at_a_time": t_seq, "batch": t_batch},
+            "clocks": clk, "trials": st["trials"]}
 
 
 def cpu_baseline(wl_name, target_s, size=None):

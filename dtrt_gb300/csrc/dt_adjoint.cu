@@ -22,6 +22,16 @@ namespace dt {
         }                                                                            \
     } while (0)
 
+// one replay launch (shared with the batch schedules, so every caller runs this unit's
+// compilation of the kernel)
+cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const float *dimg, float *grad, double *img_acc,
+                           unsigned long long *ctr, long long stride, cudaStream_t st) {
+    const long long n = (rp.path_count + stride - 1) / stride;
+    if (n <= 0) return cudaSuccess;
+    k_adjoint<1><<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, st>>>(sc, rp, dimg, grad, img_acc, ctr, stride);
+    return cudaGetLastError();
+}
+
 int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
                    int on_device, cudaStream_t st) {
     using clk = std::chrono::steady_clock;
@@ -102,10 +112,8 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     for (long long b0 = 0; b0 < total; b0 += B) {
         rp.path_begin = b0;
         rp.path_count = std::min(B, total - b0);
-        k_adjoint<1><<<(unsigned)((rp.path_count + kBlock - 1) / kBlock), kBlock, 0, st>>>(sc, rp, dimg, grad, img_acc,
-                                                                                         ctr);
+        DT_ACK(launch_adjoint(sc, rp, dimg, grad, img_acc, ctr, 1, st));
         ++launches;
-        DT_ACK(cudaGetLastError());
     }
     DT_ACK(cudaEventRecord(e1, st));
     if (image) {

@@ -205,20 +205,31 @@ int launch_once(dtrt_batch *b, const std::vector<int> &order, int chunk, long lo
 
 // one k_adjoint launch per item (every stride-th path), items dealt round-robin in `order`
 // to st and S-1 side streams that fork from and join back into st (graph-capturable)
-int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long stride, cudaStream_t st) {
+int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long stride, cudaStream_t st,
+                 bool zero = false) {
     S = std::max(1, std::min(S, 1 + (int)b->side.size()));
     if (S > 1) {
         DT_BCK(cudaEventRecord(b->fork_ev, st));
         for (int k = 1; k < S; ++k) DT_BCK(cudaStreamWaitEvent(b->side[k - 1], b->fork_ev, 0));
     }
     for (size_t i = 0; i < order.size(); ++i) {
-        const BatchItemDev &it = b->host_items[order[i]];
-        const long long n = (it.rp.path_count + stride - 1) / stride;
-        if (n <= 0) continue;
+        const int item = order[i];
+        const BatchItemDev &it = b->host_items[item];
         cudaStream_t q = (i % S == 0) ? st : b->side[i % S - 1];
-        k_adjoint<1><<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, q>>>(it.sc, it.rp, it.dimg, it.grad, it.img_acc,
-                                                                              nullptr, stride);
-        DT_BCK(cudaGetLastError());
+        if (zero) {  // each item's outputs are cleared just before its own launches, on its stream
+            if (it.img_acc) DT_BCK(cudaMemsetAsync(it.img_acc, 0, b->npix[item] * 3 * 8, q));
+            if (it.grad) DT_BCK(cudaMemsetAsync(it.grad, 0, b->nvox[item] * 4, q));
+        }
+        if (stride > 1) {
+            DT_BCK(launch_adjoint(it.sc, it.rp, it.dimg, it.grad, it.img_acc, nullptr, stride, q));
+            continue;
+        }
+        RenderParams rp = it.rp;  // launches of at most 2^24 paths, as dtrt_render_adjoint
+        for (long long b0 = 0; b0 < it.rp.path_count; b0 += 1ll << 24) {
+            rp.path_begin = b0;
+            rp.path_count = std::min(1ll << 24, it.rp.path_count - b0);
+            DT_BCK(launch_adjoint(it.sc, rp, it.dimg, it.grad, it.img_acc, nullptr, 1, q));
+        }
     }
     for (int k = 1; k < S; ++k) {
         DT_BCK(cudaEventRecord(b->side_ev[k - 1], b->side[k - 1]));
@@ -228,12 +239,13 @@ int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long 
 }
 
 int launch_schedule(dtrt_batch *b, cudaStream_t st, long long stride) {
-    if (b->schedule == 1) return launch_items(b, b->order, b->nstreams, stride, st);
+    if (b->schedule == 1) return launch_items(b, b->order, b->nstreams, stride, st, true);
     return launch_once(b, b->order, b->chunk, stride, st);
 }
 
+// clear every item's outputs (the per-item schedule clears each item just before it instead)
 int zero_outputs(dtrt_batch *b, cudaStream_t st) {
-    for (int i = 0; i < b->n; ++i) {
+    for (int i = 0; i < b->n && b->schedule != 1; ++i) {
         if (b->host_items[i].img_acc) DT_BCK(cudaMemsetAsync(b->host_items[i].img_acc, 0, b->npix[i] * 3 * 8, st));
         if (b->host_items[i].grad) DT_BCK(cudaMemsetAsync(b->host_items[i].grad, 0, b->nvox[i] * 4, st));
     }
@@ -398,7 +410,8 @@ int capture(dtrt_batch *b) {
     if (rc) return rc;
     DT_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     rc = zero_outputs(b, cs);
-    if (!rc) rc = b->schedule == 1 ? launch_items(b, b->order, b->nstreams, 1, cs) : launch_kernel(b, total, b->chunk, 1, cs);
+    if (!rc) rc = b->schedule == 1 ? launch_items(b, b->order, b->nstreams, 1, cs, true)
+                                   : launch_kernel(b, total, b->chunk, 1, cs);
     if (!rc && b->n_img > 0) {
         k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, cs>>>(b->d_imgs, b->n_img, b->total_pix);
         if (cudaGetLastError() != cudaSuccess) rc = DTRT_ERR_CUDA;

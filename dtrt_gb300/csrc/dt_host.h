@@ -51,6 +51,8 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
 bool ensure_buffer(void **ptr, size_t *have, size_t need);
 int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
                    int on_device, cudaStream_t stream);
+cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const float *dimg, float *grad, double *img_acc,
+                           unsigned long long *ctr, long long stride, cudaStream_t st);
 int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image,
                           float *d_vertices, int on_device, cudaStream_t stream);
 template <int N>

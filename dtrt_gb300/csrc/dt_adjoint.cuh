@@ -31,9 +31,15 @@ namespace dt {
 
 // One camera path of k_camera's loop, value-only, with adjoint scattering in pass B.
 // Must consume the RNG exactly like k_camera: every branch below mirrors it.
+// Event values of pass A kept for pass B (per thread): pass B then runs each NEE or
+// emitter-hit query once, with the weight known beforehand. Events past the capacity use
+// the rewind of the RNG state instead.
+constexpr int kReplayEvents = 40;
+
 template <int N>
 DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, long long g, int pixel, bool pass_b,
-                        float3 total, float3 gpix, AdjCtx &adj, Ctr &c) {
+                        float3 total, float3 gpix, AdjCtx &adj, Ctr &c, float3 *ev) {
+    int ne = 0;  // event index, in path order (identical in both passes)
     const float3 zero = mk(0.f, 0.f, 0.f);
     const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
     Rng rng;
@@ -68,46 +74,67 @@ DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, 
             DV<N> wo;
             float pdf_nee;
             if (mode & MODE_VOLUME_MAIN) {
-                const Rng saved = rng;
-                DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
-                float3 e = zero;
-                if (!v.is_zero()) {
-                    const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
-                    if (pv.v > kEps) e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
-                }
-                if (pass_b && !is_zero3(e, 0.f)) {
-                    const Rng after = rng;
-                    rng = saved;
+                const int k = ne++;
+                if (pass_b && k < kReplayEvents) {
+                    const float3 e = ev[k];
                     adj.w = dot(gpix, e) * rp.inv_spp;
-                    DV<N> wo2;
-                    float pdf2;
-                    nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
-                    rng = after;
+                    nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c,
+                                    is_zero3(e, 0.f) ? nullptr : hook);
+                    acc = acc + e;
+                } else {
+                    const Rng saved = rng;
+                    DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
+                    float3 e = zero;
+                    if (!v.is_zero()) {
+                        const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+                        if (pv.v > kEps)
+                            e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
+                    }
+                    if (pass_b && !is_zero3(e, 0.f)) {
+                        const Rng after = rng;
+                        rng = saved;
+                        adj.w = dot(gpix, e) * rp.inv_spp;
+                        DV<N> wo2;
+                        float pdf2;
+                        nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                        rng = after;
+                    }
+                    if (!pass_b && k < kReplayEvents) ev[k] = e;
+                    acc = acc + e;
                 }
-                acc = acc + e;
             }
             const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
             if (pvs.v > kEps) {
                 const float3 thr1 = thr.val() * pvs.v;
                 ray.d = wo;
                 ItsAD<N> its1;
-                const Rng saved = rng;
-                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
-                                                   nullptr, c);
-                float3 e = zero;
-                if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
-                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
-                if (pass_b && !is_zero3(e, 0.f)) {
-                    const Rng after = rng;
-                    rng = saved;
+                const int k = ne++;
+                if (pass_b && k < kReplayEvents) {
+                    const float3 e = ev[k];
                     adj.w = dot(gpix, e) * rp.inv_spp;
-                    ItsAD<N> its2;
-                    float pdf2;
-                    look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr, c,
-                                           hook);
-                    rng = after;
+                    look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr, nullptr,
+                                           c, is_zero3(e, 0.f) ? nullptr : hook);
+                    acc = acc + e;
+                } else {
+                    const Rng saved = rng;
+                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee,
+                                                       nullptr, nullptr, c);
+                    float3 e = zero;
+                    if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+                        e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+                    if (pass_b && !is_zero3(e, 0.f)) {
+                        const Rng after = rng;
+                        rng = saved;
+                        adj.w = dot(gpix, e) * rp.inv_spp;
+                        ItsAD<N> its2;
+                        float pdf2;
+                        look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr,
+                                               c, hook);
+                        rng = after;
+                    }
+                    if (!pass_b && k < kReplayEvents) ev[k] = e;
+                    acc = acc + e;
                 }
-                acc = acc + e;
                 its = its1;
                 P = cmul(P, thr1);
                 depth -= 1;
@@ -130,24 +157,34 @@ DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, 
         DV<N> wo;
         float pdf_nee;
         if (!is_null && (mode & MODE_SURFACE_MAIN)) {
-            const Rng saved = rng;
-            DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
-            float3 e = zero;
-            if (!v.is_zero()) {
-                const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
-                const float bp = bsdf_pdf(b, its0.wi, wo.val());
-                e = cmul(cmul(Q, v.val()), bv.val()) * mis_weight(pdf_nee, bp);
-            }
-            if (pass_b && !is_zero3(e, 0.f)) {
-                const Rng after = rng;
-                rng = saved;
+            const int k = ne++;
+            if (pass_b && k < kReplayEvents) {
+                const float3 e = ev[k];
                 adj.w = dot(gpix, e) * rp.inv_spp;
-                DV<N> wo2;
-                float pdf2;
-                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
-                rng = after;
+                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c,
+                                  is_zero3(e, 0.f) ? nullptr : hook);
+                acc = acc + e;
+            } else {
+                const Rng saved = rng;
+                DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+                float3 e = zero;
+                if (!v.is_zero()) {
+                    const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
+                    const float bp = bsdf_pdf(b, its0.wi, wo.val());
+                    e = cmul(cmul(Q, v.val()), bv.val()) * mis_weight(pdf_nee, bp);
+                }
+                if (pass_b && !is_zero3(e, 0.f)) {
+                    const Rng after = rng;
+                    rng = saved;
+                    adj.w = dot(gpix, e) * rp.inv_spp;
+                    DV<N> wo2;
+                    float pdf2;
+                    nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                    rng = after;
+                }
+                if (!pass_b && k < kReplayEvents) ev[k] = e;
+                acc = acc + e;
             }
-            acc = acc + e;
         }
         float bpdf, beta;
         const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
@@ -162,24 +199,34 @@ DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, 
             if (is_null) {
                 ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
             } else {
-                const Rng saved = rng;
-                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee, nullptr,
-                                                   nullptr, c);
                 thr1 = cmul(thr1, bw.val());
-                float3 e = zero;
-                if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
-                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(bpdf, pdf_nee);
-                if (pass_b && !is_zero3(e, 0.f)) {
-                    const Rng after = rng;
-                    rng = saved;
+                const int k = ne++;
+                if (pass_b && k < kReplayEvents) {
+                    const float3 e = ev[k];
                     adj.w = dot(gpix, e) * rp.inv_spp;
-                    ItsAD<N> its2;
-                    float pdf2;
-                    look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its2, pdf2, nullptr, nullptr, c,
-                                           hook);
-                    rng = after;
+                    look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee, nullptr, nullptr,
+                                           c, is_zero3(e, 0.f) ? nullptr : hook);
+                    acc = acc + e;
+                } else {
+                    const Rng saved = rng;
+                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee,
+                                                       nullptr, nullptr, c);
+                    float3 e = zero;
+                    if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
+                        e = cmul(cmul(P, thr1), att.val()) * mis_weight(bpdf, pdf_nee);
+                    if (pass_b && !is_zero3(e, 0.f)) {
+                        const Rng after = rng;
+                        rng = saved;
+                        adj.w = dot(gpix, e) * rp.inv_spp;
+                        ItsAD<N> its2;
+                        float pdf2;
+                        look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its2, pdf2, nullptr,
+                                               nullptr, c, hook);
+                        rng = after;
+                    }
+                    if (!pass_b && k < kReplayEvents) ev[k] = e;
+                    acc = acc + e;
                 }
-                acc = acc + e;
                 mode &= ~MODE_EMISSION;
             }
             its = its1;
@@ -203,13 +250,14 @@ DT_D void adjoint_one(const DevScene &sc, const RenderParams &rp, int *stack, lo
     const long long g = rp.path_begin + (active ? gi * stride : 0);
     const int pixel = (int)(g / rp.spp);
     AdjCtx adj{grad, 0.f};
+    float3 ev[kReplayEvents];
     float3 total = mk(0.f, 0.f, 0.f);
     if (active) {
-        total = replay_path<N>(sc, rp, stack, g, pixel, false, total, total, adj, c);
+        total = replay_path<N>(sc, rp, stack, g, pixel, false, total, total, adj, c, ev);
         if (grad != nullptr && dimg != nullptr && !is_zero3(total, 0.f)) {
             const float3 gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1),
                                  __ldg(dimg + 3 * (size_t)pixel + 2));
-            if (!is_zero3(gp, 0.f)) replay_path<N>(sc, rp, stack, g, pixel, true, total, gp, adj, c);
+            if (!is_zero3(gp, 0.f)) replay_path<N>(sc, rp, stack, g, pixel, true, total, gp, adj, c, ev);
         }
     }
     if (img_acc != nullptr) {

@@ -295,6 +295,17 @@ class RenderOptions:
                                   int(self.quiet), self.mode, self.ddistCoeff)
 
 
+def _stream():
+    """torch's current CUDA stream (the render runs and blocks on it), or the default stream."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    except ImportError:
+        pass
+    return None
+
+
 class Integrator:
     name = "Integrator"
 
@@ -312,7 +323,7 @@ class VolPathTracerAD(Integrator):
         lib = _abi.load()
         o = options._c()
         _abi.check(lib.dtrt_render_fwd(scene.native.handle, ctypes.byref(o), ctypes.c_void_p(_addr(rendered_image)),
-                                       0, None))
+                                       0, _stream()))
 
 
 class VolPathTracer(Integrator):
@@ -327,7 +338,7 @@ class VolPathTracer(Integrator):
         lib = _abi.load()
         dst = (ctypes.c_float * n).from_address(_addr(rendered_image))
         _abi.check(lib.dtrt_render_primal(scene.native.handle, ctypes.byref(o), ctypes.cast(dst, ctypes.c_void_p), 0,
-                                          None))
+                                          _stream()))
 
 
 class DirectIntegrator(Integrator):
@@ -379,4 +390,4 @@ class DirectAD(VolPathTracerAD):
         o.max_bounces = 1
         lib = _abi.load()
         _abi.check(lib.dtrt_render_fwd(scene.native.handle, ctypes.byref(o), ctypes.c_void_p(_addr(rendered_image)),
-                                       0, None))
+                                       0, _stream()))

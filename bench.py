@@ -295,6 +295,8 @@ def run_gpu(args, wl_name, rank, world, local_rank):
         line["grad_rmse_c2"] = grad_rmse_c2()
     if rank == 0 and not args.no_batch:
         line["batch_c4"] = batch_c4()
+    if rank == 0 and not args.no_update:
+        line["scene_update_c2"] = scene_update_c2()
     scene.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -590,6 +592,59 @@ def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2, tune_full=True):
             "clocks": clk, "trials": st["trials"]}
 
 
+# --------------------------------------------------------------------------- scene rebuild per optimisation step
+def scene_update_c2(iters=6, step=0.002, seed=5):
+    """Host cost of the scene rebuild an optimisation step needs on C2 (20,480-triangle
+    sphere, 256x256, nder 8), the vertices moved along their normals by a small random step
+    each iteration: a new scene (BVH build, edge search, allocations and copies) against an
+    in-place update (refit BVH, cached edge adjacency, arrays rewritten in place) and an
+    in-place update with the BVH built again. Wall time, description conversion included."""
+    import time
+    from dtrt_gb300 import native, scenes
+    spec = scenes.config2(256, 256, subdiv=5, nder=8)
+    v = spec.shapes[0].vertices.copy()
+    nrm = scenes.vertex_normals(v, spec.shapes[0].indices)
+    rng = np.random.default_rng(seed)
+    steps = []
+    for _ in range(iters):
+        v = (v + nrm * rng.normal(0.0, step, size=(v.shape[0], 1))).astype(np.float32)
+        steps.append(v)
+
+    def timed(fn):
+        t = time.perf_counter()
+        r = fn()
+        return (time.perf_counter() - t) * 1e3, r
+
+    ns = native.NativeScene(spec)
+    native.NativeScene(spec).close()  # first-use costs out of the timings
+    create, refit, rebuild, stats = [], [], [], []
+    for vk in steps:
+        spec.shapes[0].vertices = vk
+        ms, sc = timed(lambda: native.NativeScene(spec))
+        sc.close()
+        create.append(ms)
+    spec.shapes[0].vertices = v.copy()
+    for vk in steps:
+        spec.shapes[0].vertices = vk
+        ms, st = timed(lambda: ns.update(spec))
+        refit.append(ms)
+        stats.append(st)
+    for vk in steps:
+        spec.shapes[0].vertices = vk
+        ms, _ = timed(lambda: ns.update(spec, rebuild_bvh=True))
+        rebuild.append(ms)
+    ns.close()
+    med = lambda a: float(np.median(a))
+    return {"workload": f"C2 sphere, {sum(sh.indices.shape[0] for sh in spec.shapes)} triangles, 256x256, nder 8: "
+                        f"{iters} steps of normal displacement (sigma {step})",
+            "create_ms": med(create), "update_refit_ms": med(refit), "update_rebuild_bvh_ms": med(rebuild),
+            "speedup_refit_vs_create": med(create) / med(refit),
+            "bvh_refit": [s["bvh_refit"] for s in stats], "sah_ratio_last": stats[-1]["sah_ratio"],
+            "buffers_reused": stats[-1]["buffers_reused"], "buffers_allocated": stats[-1]["buffers_allocated"],
+            "host_ms_inside_update": med([s["host_ms"] for s in stats]),
+            "update_phases_ms": {k: med([s[k] for s in stats]) for k in ("ms_bvh", "ms_arrays", "ms_device")}}
+
+
 def cpu_baseline(wl_name, target_s, size=None):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
@@ -618,6 +673,7 @@ def main():
     ap.add_argument("--grad-size", type=int, default=None, help="image side of the gradient leg (default 512)")
     ap.add_argument("--adjoint-only", action="store_true", help="time only the C3 density adjoint replay")
     ap.add_argument("--no-batch", action="store_true", help="skip the C4 batch leg")
+    ap.add_argument("--no-update", action="store_true", help="skip the C2 scene rebuild leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -173,6 +173,18 @@ class BatchStats(ctypes.Structure):
                 "order": list(self.order[:min(n, BATCH_MAX_ITEMS)])}
 
 
+UPDATE_REBUILD_BVH = 1
+
+
+class UpdateStats(ctypes.Structure):
+    _fields_ = [("bvh_refit", ctypes.c_int), ("buffers_reused", ctypes.c_int), ("buffers_allocated", ctypes.c_int),
+                ("sah_ratio", ctypes.c_float), ("host_ms", ctypes.c_double), ("ms_bvh", ctypes.c_double),
+                ("ms_arrays", ctypes.c_double), ("ms_device", ctypes.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # Every C-ABI symbol declared in include/dtrt_gb300.h, with its ctypes signature.
 EST_SCATTER_SEGMENT_FROM_ORIGIN = 1
 
@@ -184,6 +196,8 @@ _SIGNATURES = {
     "dtrt_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "dtrt_scene_set_edge_weights": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int]),
     "dtrt_scene_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dtrt_scene_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SceneDesc), ctypes.c_uint,
+                                         ctypes.POINTER(UpdateStats)]),
     "dtrt_render_fwd": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,
                                        ctypes.c_int, ctypes.c_void_p]),
     "dtrt_render_fwd_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,

@@ -8,12 +8,14 @@
 // (src/edge_manager/bruteforce.cpp:4-20) and primary-edge projection
 // (src/edge_manager/edge_manager.cpp:6-110, include/line_clip.h:37-95).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "dt_bvh.h"
@@ -140,26 +142,85 @@ int read_vol(const char *path, int res[3], int &ch, float vmin[3], float vmax[3]
     return DTRT_OK;
 }
 
+// Device uploads of one scene build. Every upload call takes the next slot of
+// s->allocs (an empty array takes a null slot), so two builds of scenes with the same
+// structure issue their arrays in the same slot order. Given the allocations of the scene
+// being replaced (`reuse`, in that slot order), an upload of the same byte size takes the
+// old buffer, and the copy is deferred to commit(): nothing on the device changes until
+// the whole host build has succeeded.
 struct Builder {
+    struct Slot {
+        void *p;
+        size_t bytes;
+    };
     dtrt_scene *s;
-    explicit Builder(dtrt_scene *sc) : s(sc) {}
+    std::vector<Slot> *reuse = nullptr;
+    std::vector<std::pair<void *, std::vector<char>>> pending;
+    std::vector<char> taken;  // per slot of s->allocs: the buffer came from `reuse`
+    int reused = 0, allocated = 0;
+    double ms_alloc = 0.0;
+    explicit Builder(dtrt_scene *sc, std::vector<Slot> *old = nullptr) : s(sc), reuse(old) {}
     template <class T>
     bool upload(const std::vector<T> &v, const T **dst) {
-        if (v.empty()) {
-            *dst = nullptr;
-            return true;
-        }
+        const size_t k = s->allocs.size(), bytes = v.size() * sizeof(T);
         void *p = nullptr;
-        cudaError_t e = cudaMalloc(&p, v.size() * sizeof(T));
-        if (e == cudaSuccess) e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
-            set_last_error(std::string("scene upload: ") + cudaGetErrorString(e));
-            if (p) cudaFree(p);
-            return false;
+        bool from_old = false;
+        if (bytes) {
+            if (reuse && k < reuse->size() && (*reuse)[k].p && (*reuse)[k].bytes == bytes) {
+                p = (*reuse)[k].p;
+                (*reuse)[k].p = nullptr;
+                from_old = true;
+                ++reused;
+            } else {
+                const auto ta = std::chrono::steady_clock::now();
+                cudaError_t e = cudaMalloc(&p, bytes);
+                ms_alloc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - ta).count();
+                if (e != cudaSuccess) {
+                    set_last_error(std::string("scene upload: ") + cudaGetErrorString(e));
+                    return false;
+                }
+                ++allocated;
+            }
         }
         s->allocs.push_back(p);
+        s->alloc_bytes.push_back(bytes);
+        taken.push_back(from_old ? 1 : 0);
         *dst = (const T *)p;
+        if (!bytes) return true;
+        if (reuse) {
+            const char *b = reinterpret_cast<const char *>(v.data());
+            pending.emplace_back(p, std::vector<char>(b, b + bytes));
+            return true;
+        }
+        cudaError_t e = cudaMemcpy(p, v.data(), bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            set_last_error(std::string("scene upload: ") + cudaGetErrorString(e));
+            return false;
+        }
         return true;
+    }
+    // deferred copies (reuse mode)
+    int commit() {
+        for (auto &pc : pending) {
+            cudaError_t e = cudaMemcpy(pc.first, pc.second.data(), pc.second.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) {
+                set_last_error(std::string("scene upload: ") + cudaGetErrorString(e));
+                return DTRT_ERR_CUDA;
+            }
+        }
+        pending.clear();
+        return DTRT_OK;
+    }
+    // a failed reuse-mode build: free what it allocated, hand the taken buffers back
+    void discard() {
+        for (size_t k = 0; k < s->allocs.size(); ++k) {
+            if (taken[k]) (*reuse)[k].p = s->allocs[k];
+            else if (s->allocs[k]) cudaFree(s->allocs[k]);
+        }
+        s->allocs.clear();
+        s->alloc_bytes.clear();
+        taken.clear();
+        pending.clear();
     }
 };
 
@@ -265,13 +326,44 @@ bool load_grid(DevGrid &g, Builder &bld, const char *file, const float *arr, con
     return true;
 }
 
-int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
+// fn(i) for i in [0, n) on up to 16 host threads in contiguous chunks of at least `grain`;
+// fn writes only to slot i of preallocated outputs, so results do not depend on the threads.
+template <class F>
+void parallel_for(int n, int grain, F &&fn) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int nt = std::min(std::min((int)(hw ? hw : 1), 16), (n + grain - 1) / std::max(grain, 1));
+    if (nt <= 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    const int chunk = (n + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) {
+        const int lo = t * chunk, hi = std::min(n, lo + chunk);
+        if (lo >= hi) break;
+        try {
+            th.emplace_back([&fn, lo, hi] {
+                for (int i = lo; i < hi; ++i) fn(i);
+            });
+        } catch (...) {  // no thread to be had: run that chunk here
+            for (int i = lo; i < hi; ++i) fn(i);
+        }
+    }
+    for (int i = 0; i < std::min(n, chunk); ++i) fn(i);
+    for (auto &x : th) x.join();
+}
+
+// Build the device scene from a description. With s->topo valid (a rebuild of a scene
+// with the same triangles) the edge adjacency is taken from it and the BVH is refit unless
+// `rebuild_bvh`; `info` (optional) reports which.
+int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebuild_bvh, dtrt_update_stats *info) {
     const int N = d->nder;
     DevScene &ds = s->dev;
     std::memset(&ds, 0, sizeof(ds));
     ds.nder = N;
     ds.tracking_cap = 10000;
-    Builder bld(s);
+    SceneTopology &tp = s->topo;
+    const bool cached = tp.valid;
     auto fail = [](const std::string &m) {
         set_last_error(m);
         return DTRT_ERR_INVALID;
@@ -382,17 +474,24 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
             for (int k = 0; k < 3; ++k)
                 if (f[k] < 0 || f[k] >= sh.nv) return fail("triangle index out of range");
             tris.push_back(make_int4(vtot + f[0], vtot + f[1], vtot + f[2], si));
-            // face normal with derivatives, shape.cpp:109-126
-            HV n = hcross(vad[si][f[1]] - vad[si][f[0]], vad[si][f[2]] - vad[si][f[0]]);
+        }
+        // face normals with derivatives, shape.cpp:109-126 (one slot per triangle, host threads)
+        facen.resize((size_t)ttot + sh.nt);
+        if (any_vel) fder.resize(((size_t)ttot + sh.nt) * N * 3);
+        const std::vector<HV> &vs = vad[si];
+        parallel_for(sh.nt, 2048, [&](int t) {
+            const int *f = sd.indices + 3 * t;
+            HV n = hcross(vs[f[1]] - vs[f[0]], vs[f[2]] - vs[f[0]]);
             HD len = hsqrt(hdot(n, n));
             if (len.v >= 1e-7) n = n / len;
-            facen.push_back(make_float4((float)n.x.v, (float)n.y.v, (float)n.z.v, 0.f));
+            const size_t ft = (size_t)ttot + t;
+            facen[ft] = make_float4((float)n.x.v, (float)n.y.v, (float)n.z.v, 0.f);
             for (int j = 0; j < N && any_vel; ++j) {
-                fder.push_back((float)n.x.d[j]);
-                fder.push_back((float)n.y.d[j]);
-                fder.push_back((float)n.z.d[j]);
+                fder[(ft * N + j) * 3 + 0] = (float)n.x.d[j];
+                fder[(ft * N + j) * 3 + 1] = (float)n.y.d[j];
+                fder[(ft * N + j) * 3 + 2] = (float)n.z.d[j];
             }
-        }
+        });
         vtot += sh.nv;
         ttot += sh.nt;
     }
@@ -405,36 +504,46 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
     std::vector<double> edge_cdf;
     s->shape_edge_len.assign(d->num_shapes, 0.f);
     s->shape_skip.assign(d->num_shapes, 0);
+    if (!cached) {  // edge adjacency from the triangle lists: sorted unique vertex pairs and their faces
+        tp.adj.clear();
+        tp.adj_off.assign(1, 0);
+        for (int si = 0; si < d->num_shapes; ++si) {
+            const DevShape &sh = shapes[si];
+            std::map<std::pair<int, int>, std::vector<int>> m;
+            for (int t = 0; t < sh.nt; ++t) {
+                const int4 tr = tris[sh.tri_off + t];
+                const int ids[3] = {tr.x - sh.vert_off, tr.y - sh.vert_off, tr.z - sh.vert_off};
+                for (int e = 0; e < 3; ++e) {
+                    int a = ids[e], b = ids[(e + 1) % 3];
+                    m[a < b ? std::make_pair(a, b) : std::make_pair(b, a)].push_back(t);
+                }
+            }
+            for (auto const &kv : m) {
+                if (kv.second.size() > 2) return fail("non-manifold mesh: an edge is shared by more than 2 faces");
+                if (kv.second.size() == 2 && kv.second[0] == kv.second[1]) return fail("duplicated faces");
+                tp.adj.push_back(make_int4(kv.first.first, kv.first.second, kv.second[0],
+                                           kv.second.size() == 2 ? kv.second[1] : -1));
+            }
+            tp.adj_off.push_back((int)tp.adj.size());
+        }
+    }
     for (int si = 0; si < d->num_shapes; ++si) {
         DevShape &sh = shapes[si];
-        std::map<std::pair<int, int>, std::vector<int>> m;
-        for (int t = 0; t < sh.nt; ++t) {
-            const int4 tr = tris[sh.tri_off + t];
-            const int ids[3] = {tr.x - sh.vert_off, tr.y - sh.vert_off, tr.z - sh.vert_off};
-            for (int e = 0; e < 3; ++e) {
-                int a = ids[e], b = ids[(e + 1) % 3];
-                m[a < b ? std::make_pair(a, b) : std::make_pair(b, a)].push_back(t);
-            }
-        }
         sh.edge_off = (int)edges.size();
         sh.edge_cdf_off = (int)edge_cdf.size();
         double sum = 0;
         std::vector<double> lens;
-        for (auto const &kv : m) {
-            const float4 va = verts[sh.vert_off + kv.first.first], vb = verts[sh.vert_off + kv.first.second];
+        for (int k = tp.adj_off[si]; k < tp.adj_off[si + 1]; ++k) {
+            const int4 ad = tp.adj[k];
+            const float4 va = verts[sh.vert_off + ad.x], vb = verts[sh.vert_off + ad.y];
             const double len = dnorm({(double)va.x - vb.x, (double)va.y - vb.y, (double)va.z - vb.z});
-            DevEdge e{sh.vert_off + kv.first.first, sh.vert_off + kv.first.second, -1, -1, si, (float)len};
-            if (kv.second.size() > 2) return fail("non-manifold mesh: an edge is shared by more than 2 faces");
-            if (kv.second.size() == 2) {
-                if (kv.second[0] == kv.second[1]) return fail("duplicated faces");
-                const float4 n0 = facen[sh.tri_off + kv.second[0]], n1 = facen[sh.tri_off + kv.second[1]];
+            DevEdge e{sh.vert_off + ad.x, sh.vert_off + ad.y, sh.tri_off + ad.z, -1, si, (float)len};
+            if (ad.w >= 0) {
+                const float4 n0 = facen[sh.tri_off + ad.z], n1 = facen[sh.tri_off + ad.w];
                 const double cc = (double)n0.x * n1.x + (double)n0.y * n1.y + (double)n0.z * n1.z;
                 if (cc < -1.0 + 1e-7) return fail("inconsistent normal orientation");
                 if (!(cc < 1.0 - 1e-7)) continue;  // flat edge
-                e.f0 = sh.tri_off + kv.second[0];
-                e.f1 = sh.tri_off + kv.second[1];
-            } else {
-                e.f0 = sh.tri_off + kv.second[0];
+                e.f1 = sh.tri_off + ad.w;
             }
             edges.push_back(e);
             lens.push_back(len);
@@ -459,10 +568,32 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
             const float vv[9] = {a.x, a.y, a.z, b.x, b.y, b.z, cc.x, cc.y, cc.z};
             std::memcpy(&tv[9 * (size_t)t], vv, sizeof(vv));
         }
-        BvhBuildOut bo;
-        build_bvh(tv, ttot, bo);
-        ds.num_nodes = (int)bo.nodes.size();
-        if (!bld.upload(bo.nodes, &ds.nodes) || !bld.upload(bo.leaf_tris, &ds.leaf_tris)) return DTRT_ERR_CUDA;
+        // refit while the surface-area cost stays within kRefitCostLimit of the cost at the
+        // last full build; past it (or when asked) build the tree again. The cost is relative
+        // to the root box, so shape changes that a new tree cannot undo (a stretch) raise it
+        // too: on a 5,120-triangle sphere a 3x stretch gave 1.9x for the refit tree and the
+        // same cost for a new one, while folds that interleave distant parts gave 3-6x, where
+        // a new tree halves the cost.
+        constexpr double kRefitCostLimit = 2.0;
+        const auto tb = std::chrono::steady_clock::now();
+        bool refit = cached && !rebuild_bvh && !tp.bvh.nodes.empty();
+        double ratio = 1.0;
+        if (refit) {
+            refit_bvh(tv, tp.bvh);
+            ratio = tp.sah_build > 0.0 ? bvh_sah_cost(tp.bvh) / tp.sah_build : 1.0;
+            if (!(ratio <= kRefitCostLimit)) refit = false;
+        }
+        if (!refit) {
+            build_bvh(tv, ttot, tp.bvh);
+            tp.sah_build = bvh_sah_cost(tp.bvh);
+        }
+        if (info) {
+            info->bvh_refit = refit ? 1 : 0;
+            info->sah_ratio = (float)ratio;
+            info->ms_bvh = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
+        }
+        ds.num_nodes = (int)tp.bvh.nodes.size();
+        if (!bld.upload(tp.bvh.nodes, &ds.nodes) || !bld.upload(tp.bvh.leaf_tris, &ds.leaf_tris)) return DTRT_ERR_CUDA;
     }
     // ------------------------------------------------------------ materials
     std::vector<DevBsdf> bsdfs(d->num_bsdfs);
@@ -569,6 +700,11 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
         } else {
             return fail("unknown medium type");
         }
+        if (cached && (tp.media_type[mi] != o.type ||
+                       (o.type == MEDIUM_HETEROGENEOUS && (tp.media_res[3 * mi] != o.density.res[0] ||
+                                                           tp.media_res[3 * mi + 1] != o.density.res[1] ||
+                                                           tp.media_res[3 * mi + 2] != o.density.res[2]))))
+            return fail("scene update: a medium changed its type or grid resolution");
     }
     // ------------------------------------------------------------ light tables, scene.cpp:45-98
     std::vector<float> light_pmf(d->num_emitters), light_cdf(d->num_emitters), light_area(d->num_emitters), area_cdf;
@@ -609,11 +745,27 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
     std::vector<float> pjac;
     std::vector<int> pverts;
     const double aspect = (double)c.width / c.height, fov = c2ndc[0];
+    // every edge is projected on its own (host threads, one output slot per candidate
+    // edge), then the kept ones are gathered in edge order: the same arrays as a serial loop
+    struct PEdgeOut {
+        DevPrimaryEdge pe;
+        float jac[24];
+        bool ok;
+    };
+    std::vector<int2> cand;  // (shape, edge of the shape)
     for (int si = 0; si < d->num_shapes; ++si) {
         const DevShape &sh = shapes[si];
         if (bsdfs[sh.bsdf_id].type == BSDF_NULL && sh.light_id < 0) continue;
-        for (int k = 0; k < sh.num_edges; ++k) {
-            const DevEdge &e = edges[sh.edge_off + k];
+        for (int k = 0; k < sh.num_edges; ++k) cand.push_back(make_int2(si, k));
+    }
+    std::vector<PEdgeOut> pout(cand.size());
+    parallel_for((int)cand.size(), 1024, [&](int ci) {
+        PEdgeOut &po = pout[ci];
+        po.ok = false;
+        const int si = cand[ci].x;
+        const DevShape &sh = shapes[si];
+        {
+            const DevEdge &e = edges[sh.edge_off + cand[ci].y];
             // silhouette test against the camera position (shape.cpp:302-335)
             if (e.f1 >= 0) {
                 const float4 a = verts[e.v0], b = verts[e.v1];
@@ -633,14 +785,14 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
                         }
                 }
                 const int sil = ff[0] != ff[1] ? 2 : (sh.has_normals ? 0 : 1);
-                if (sil <= 0) continue;
+                if (sil <= 0) return;
             }
             HV v0 = vad[si][e.v0 - sh.vert_off], v1 = vad[si][e.v1 - sh.vert_off];
             const double cn[3] = {fr[2].x, fr[2].y, fr[2].z};
             const double z0 = (v0.x.v - cpos.x) * cn[0] + (v0.y.v - cpos.y) * cn[1] + (v0.z.v - cpos.z) * cn[2];
             const double z1 = (v1.x.v - cpos.x) * cn[0] + (v1.y.v - cpos.y) * cn[1] + (v1.z.v - cpos.z) * cn[2];
             const double near = c.clip_near;
-            if (z0 < near && z1 < near) continue;
+            if (z0 < near && z1 < near) return;
             if (z0 < near) v0 = v0 + (v1 - v0) * ((near - z0) / (z1 - z0));
             else if (z1 < near) v1 = v1 + (v0 - v1) * ((near - z1) / (z0 - z1));
             D3 v0l = xfm_point(w2c, val(v0)), v1l = xfm_point(w2c, val(v1));
@@ -658,7 +810,7 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
                 ymax = (double)((float)(c.crop_offset_y + c.crop_height) / c.height);
             }
             HD c0[2], c1[2];
-            if (!clip_line(r0, r1, c0, c1, xmin, xmax, ymin, ymax)) continue;
+            if (!clip_line(r0, r1, c0, c1, xmin, xmax, ymin, ymax)) return;
             D3 v0p = val(v0), v1p = val(v1);
             const D3 t0v = v0l, t1v = v1l;
             const D3 dv = sub(val(v1), val(v0));
@@ -688,8 +840,7 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
             double *dsts[4] = {pe.v0p, pe.v1p, pe.v0c, pe.v1c};
             for (int q = 0; q < 4; ++q)
                 for (int a = 0; a < 3; ++a) dsts[q][a] = srcs[q][a];
-            pedges.push_back(pe);
-            plen.push_back(std::hypot(pe.v0s[0] - pe.v1s[0], pe.v0s[1] - pe.v1s[1]));
+            po.pe = pe;
             // Jacobian of the two clipped screen endpoints (pixels) w.r.t. the edge's vertex
             // positions (dual slots 0-2: v0, 3-5: v1) for a static camera: the same near-plane
             // clip, projection and image clip as above, for the vertex-position adjoint
@@ -711,15 +862,24 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
                 HD k0[2], k1[2];
                 const bool vis = clip_line(q0, q1, k0, k1, xmin, xmax, ymin, ymax);
                 for (int q = 0; q < 6; ++q) {
-                    pjac.push_back(vis ? (float)(k0[0].d[q] * c.width) : 0.f);
+                    po.jac[q] = vis ? (float)(k0[0].d[q] * c.width) : 0.f;
+                    po.jac[6 + q] = vis ? (float)(k0[1].d[q] * c.height) : 0.f;
+                    po.jac[12 + q] = vis ? (float)(k1[0].d[q] * c.width) : 0.f;
+                    po.jac[18 + q] = vis ? (float)(k1[1].d[q] * c.height) : 0.f;
                 }
-                for (int q = 0; q < 6; ++q) pjac.push_back(vis ? (float)(k0[1].d[q] * c.height) : 0.f);
-                for (int q = 0; q < 6; ++q) pjac.push_back(vis ? (float)(k1[0].d[q] * c.width) : 0.f);
-                for (int q = 0; q < 6; ++q) pjac.push_back(vis ? (float)(k1[1].d[q] * c.height) : 0.f);
-                pverts.push_back(e.v0);
-                pverts.push_back(e.v1);
+                po.ok = true;
             }
         }
+    });
+    for (size_t ci = 0; ci < cand.size(); ++ci) {
+        const PEdgeOut &po = pout[ci];
+        if (!po.ok) continue;
+        const DevEdge &e = edges[shapes[cand[ci].x].edge_off + cand[ci].y];
+        pedges.push_back(po.pe);
+        plen.push_back(std::hypot(po.pe.v0s[0] - po.pe.v1s[0], po.pe.v0s[1] - po.pe.v1s[1]));
+        pjac.insert(pjac.end(), po.jac, po.jac + 24);
+        pverts.push_back(e.v0);
+        pverts.push_back(e.v1);
     }
     std::vector<double> pcdf;
     double psum = 0;
@@ -743,7 +903,8 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
         !bld.upload(light_area, &ds.light_area) || !bld.upload(area_cdf, &ds.area_cdf) ||
         !bld.upload(area_begin, &ds.area_cdf_begin) || !bld.upload(edges, &ds.edges) ||
         !bld.upload(edge_cdf, &ds.edge_cdf) || !bld.upload(pedges, &ds.pedges) || !bld.upload(pcdf, &ds.pedge_cdf) ||
-        !bld.upload(pjac, &ds.pedge_jac) || !bld.upload(pverts, &ds.pedge_verts))
+        !bld.upload(pjac, &ds.pedge_jac) || !bld.upload(pverts, &ds.pedge_verts) ||
+        !bld.upload(std::vector<double>(d->num_shapes + 1, 0.0), &ds.shape_edge_cdf))  // filled by set_edge_weights
         return DTRT_ERR_CUDA;
     if (!any_normals) ds.normal_der = nullptr;
     ds.num_bsdfs = d->num_bsdfs;
@@ -755,6 +916,48 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d) {
     s->num_shapes = d->num_shapes;
     for (int si = 0; si < d->num_shapes; ++si)
         s->shape_skip[si] = (bsdfs[shapes[si].bsdf_id].type == BSDF_NULL && shapes[si].light_id < 0) ? 1 : 0;
+    if (!cached) {
+        tp.shape_nv.resize(d->num_shapes);
+        tp.shape_nt.resize(d->num_shapes);
+        tp.indices.clear();
+        for (int si = 0; si < d->num_shapes; ++si) {
+            tp.shape_nv[si] = shapes[si].nv;
+            tp.shape_nt[si] = shapes[si].nt;
+            tp.indices.insert(tp.indices.end(), d->shapes[si].indices, d->shapes[si].indices + 3 * (size_t)shapes[si].nt);
+        }
+        tp.media_type.resize(d->num_media);
+        tp.media_res.assign(3 * (size_t)d->num_media, 0);
+        for (int mi = 0; mi < d->num_media; ++mi) {
+            tp.media_type[mi] = media[mi].type;
+            for (int a = 0; a < 3 && media[mi].type == MEDIUM_HETEROGENEOUS; ++a) tp.media_res[3 * mi + a] = media[mi].density.res[a];
+        }
+        tp.valid = true;
+    }
+    return DTRT_OK;
+}
+
+// Same triangles as the scene was built with: derivative width, shape count, per shape
+// vertex and triangle counts and the index lists; the same number of media.
+int check_same_topology(const dtrt_scene *s, const dtrt_scene_desc *d) {
+    const SceneTopology &tp = s->topo;
+    auto fail = [](const std::string &m) {
+        set_last_error("scene update: " + m);
+        return DTRT_ERR_INVALID;
+    };
+    if (!tp.valid) return fail("the scene holds no topology");
+    if (d->nder != s->nder) return fail("nder differs from the scene's");
+    if (d->num_shapes != s->num_shapes || (d->num_shapes > 0 && !d->shapes)) return fail("the number of shapes changed");
+    if (d->num_media != (int)tp.media_type.size()) return fail("the number of media changed");
+    size_t off = 0;
+    for (int si = 0; si < d->num_shapes; ++si) {
+        const dtrt_shape_desc &sd = d->shapes[si];
+        if (sd.num_vertices != tp.shape_nv[si] || sd.num_triangles != tp.shape_nt[si] || !sd.indices)
+            return fail("shape " + std::to_string(si) + " changed its vertex or triangle count");
+        const size_t n = 3 * (size_t)sd.num_triangles;
+        if (std::memcmp(sd.indices, tp.indices.data() + off, n * sizeof(int)) != 0)
+            return fail("shape " + std::to_string(si) + " changed its triangle indices");
+        off += n;
+    }
     return DTRT_OK;
 }
 
@@ -779,21 +982,19 @@ int set_edge_weights(dtrt_scene *s, const float *w) {
     }
     if (sum > 0) cdf[s->num_shapes] = 1.0;
     s->dev.has_edges = sum > 1e-7 ? 1 : 0;
-    if (s->dev.shape_edge_cdf) {
-        cudaError_t e = cudaMemcpy((void *)s->dev.shape_edge_cdf, cdf.data(), cdf.size() * 8, cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
-            set_last_error(cudaGetErrorString(e));
-            return DTRT_ERR_CUDA;
-        }
-        return DTRT_OK;
+    cudaError_t e = cudaMemcpy((void *)s->dev.shape_edge_cdf, cdf.data(), cdf.size() * 8, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
     }
-    Builder bld(s);
-    return bld.upload(cdf, &s->dev.shape_edge_cdf) ? DTRT_OK : DTRT_ERR_CUDA;
+    return DTRT_OK;
 }
 
 void free_scene(dtrt_scene *s) {
-    for (void *p : s->allocs) cudaFree(p);
+    for (void *p : s->allocs)
+        if (p) cudaFree(p);
     s->allocs.clear();
+    s->alloc_bytes.clear();
     for (void *p : s->dgrid_bufs)
         if (p) cudaFree(p);
     s->dgrid_bufs.clear();
@@ -863,7 +1064,8 @@ int dtrt_scene_create(const dtrt_scene_desc *desc, dtrt_scene **out) {
     std::unique_ptr<dtrt_scene> s(new dtrt_scene());
     s->nder = desc->nder;
     cudaGetDevice(&s->device);
-    int st = dt::build_scene(s.get(), desc);
+    dt::Builder bld(s.get());
+    int st = dt::build_scene(s.get(), desc, bld, true, nullptr);
     if (st == DTRT_OK) st = dt::set_edge_weights(s.get(), desc->edge_weights);
     if (st != DTRT_OK) {
         dt::free_scene(s.get());
@@ -886,6 +1088,85 @@ int dtrt_scene_destroy(dtrt_scene *scene) {
     dt::free_scene(scene);
     delete scene;
     return DTRT_OK;
+}
+
+int dtrt_scene_update(dtrt_scene *scene, const dtrt_scene_desc *desc, unsigned flags, dtrt_update_stats *stats) {
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!scene || !desc) {
+        dt::set_last_error("null argument");
+        return DTRT_ERR_INVALID;
+    }
+    if (flags & ~(unsigned)DTRT_UPDATE_REBUILD_BVH) {
+        dt::set_last_error("unknown scene update flag");
+        return DTRT_ERR_INVALID;
+    }
+    int st = dt::check_same_topology(scene, desc);
+    if (st) return st;
+    if (desc->edge_weights)  // validated up front: set_edge_weights runs after the device copies
+        for (int i = 0; i < desc->num_shapes; ++i)
+            if (!(desc->edge_weights[i] >= 0.f)) {
+                dt::set_last_error("edge sampling weights must be >= 0");
+                return DTRT_ERR_INVALID;
+            }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        dt::set_last_error(std::string("scene update: ") + cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
+    }
+    // build into a fresh scene object that takes over the old arrays of unchanged size
+    std::unique_ptr<dtrt_scene> t(new dtrt_scene());
+    t->nder = scene->nder;
+    t->device = scene->device;
+    t->topo = scene->topo;
+    std::vector<dt::Builder::Slot> pool(scene->allocs.size());
+    for (size_t k = 0; k < pool.size(); ++k) pool[k] = {scene->allocs[k], scene->alloc_bytes[k]};
+    dt::Builder bld(t.get(), &pool);
+    dtrt_update_stats info{};
+    const auto t1 = std::chrono::steady_clock::now();
+    st = dt::build_scene(t.get(), desc, bld, (flags & DTRT_UPDATE_REBUILD_BVH) != 0, &info);
+    const auto t2 = std::chrono::steady_clock::now();
+    if (st == DTRT_OK) st = bld.commit();
+    if (st != DTRT_OK) {
+        bld.discard();
+        return st;
+    }
+    // state set on the scene after creation
+    t->dev.est_flags = scene->dev.est_flags;
+    t->dev.tracking_cap = scene->dev.tracking_cap;
+    bool dgrid = false;
+    for (size_t mi = 0; mi < scene->dgrid_bufs.size(); ++mi) {
+        if (!scene->dgrid_bufs[mi]) continue;  // media types and resolutions are unchanged
+        t->dgrid_bufs[mi] = scene->dgrid_bufs[mi];
+        scene->dgrid_bufs[mi] = nullptr;
+        t->media_host[mi].density.dgrid = (const float *)t->dgrid_bufs[mi];
+        t->media_host[mi].density.dgrid_n = scene->media_host[mi].density.dgrid_n;
+        dgrid = true;
+    }
+    for (auto &sl : pool)  // old arrays whose size changed
+        if (sl.p) cudaFree(sl.p);
+    for (void *p : scene->dgrid_bufs)
+        if (p) cudaFree(p);
+    scene->dev = t->dev;
+    scene->allocs.swap(t->allocs);
+    scene->alloc_bytes.swap(t->alloc_bytes);
+    scene->media_host.swap(t->media_host);
+    scene->dgrid_bufs.swap(t->dgrid_bufs);
+    scene->shape_edge_len.swap(t->shape_edge_len);
+    scene->shape_skip.swap(t->shape_skip);
+    scene->density_voxels = t->density_voxels;
+    scene->num_shapes = t->num_shapes;
+    scene->topo = std::move(t->topo);
+    st = dt::set_edge_weights(scene, desc->edge_weights);
+    if (st == DTRT_OK && dgrid) st = dt::upload_media(scene);
+    info.buffers_reused = bld.reused;
+    info.buffers_allocated = bld.allocated;
+    const auto t3 = std::chrono::steady_clock::now();
+    info.host_ms = std::chrono::duration<double, std::milli>(t3 - t0).count();
+    // allocations happen inside the build; everything after it is device work
+    info.ms_arrays = std::chrono::duration<double, std::milli>(t2 - t1).count() - info.ms_bvh - bld.ms_alloc;
+    info.ms_device = bld.ms_alloc + std::chrono::duration<double, std::milli>(t3 - t2).count();
+    if (stats) *stats = info;
+    return st;
 }
 
 int dtrt_render_fwd(dtrt_scene *scene, const dtrt_render_options *opts, float *out, int out_on_device, void *stream) {

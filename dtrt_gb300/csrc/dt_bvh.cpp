@@ -24,6 +24,13 @@ struct Box {
     }
 };
 
+// child code of a leaf: ~((first triangle << 3) | (count - 1))
+inline void leaf_range(int code, int &base, int &count) {
+    const int v = ~code;
+    base = v >> 3;
+    count = (v & 7) + 1;
+}
+
 struct Builder {
     const std::vector<float> &tv;
     std::vector<int> order;
@@ -143,6 +150,67 @@ void build_bvh(const std::vector<float> &tri_verts, int num_tris, BvhBuildOut &o
         nd.child = make_int4(code, code, 0, 0);
         out.nodes.insert(out.nodes.begin(), nd);
     }
+}
+
+void refit_bvh(const std::vector<float> &tri_verts, BvhBuildOut &tree) {
+    const int n = (int)tree.nodes.size();
+    std::vector<Box> nbox(n);
+    for (int i = n - 1; i >= 0; --i) {
+        BvhNode &nd = tree.nodes[i];
+        const int codes[2] = {nd.child.x, nd.child.y};
+        Box cb[2];
+        for (int c = 0; c < 2; ++c) {
+            if (codes[c] >= 0) {
+                cb[c] = nbox[codes[c]];
+                continue;
+            }
+            int base, count;
+            leaf_range(codes[c], base, count);
+            for (int k = base; k < base + count; ++k) {
+                float4 &a = tree.leaf_tris[3 * (size_t)k];
+                int t;
+                std::memcpy(&t, &a.w, 4);
+                const float *v = &tri_verts[9 * (size_t)t];
+                for (int q = 0; q < 3; ++q) cb[c].grow(v + 3 * q);
+                a.x = v[0]; a.y = v[1]; a.z = v[2];
+                tree.leaf_tris[3 * (size_t)k + 1] = make_float4(v[3] - v[0], v[4] - v[1], v[5] - v[2], 0.f);
+                tree.leaf_tris[3 * (size_t)k + 2] = make_float4(v[6] - v[0], v[7] - v[1], v[8] - v[2], 0.f);
+            }
+        }
+        nd.x = make_float4(cb[0].lo[0], cb[0].hi[0], cb[1].lo[0], cb[1].hi[0]);
+        nd.y = make_float4(cb[0].lo[1], cb[0].hi[1], cb[1].lo[1], cb[1].hi[1]);
+        nd.z = make_float4(cb[0].lo[2], cb[0].hi[2], cb[1].lo[2], cb[1].hi[2]);
+        nbox[i] = cb[0];
+        nbox[i].grow(cb[1]);
+    }
+}
+
+double bvh_sah_cost(const BvhBuildOut &tree) {
+    if (tree.nodes.empty()) return 0.0;
+    double inner = 0.0, leaves = 0.0, root = 0.0;
+    for (size_t i = 0; i < tree.nodes.size(); ++i) {
+        const BvhNode &nd = tree.nodes[i];
+        Box cb[2];
+        const float lo[2][3] = {{nd.x.x, nd.y.x, nd.z.x}, {nd.x.z, nd.y.z, nd.z.z}};
+        const float hi[2][3] = {{nd.x.y, nd.y.y, nd.z.y}, {nd.x.w, nd.y.w, nd.z.w}};
+        Box u;
+        for (int c = 0; c < 2; ++c) {
+            cb[c].grow(lo[c]);
+            cb[c].grow(hi[c]);
+            u.grow(cb[c]);
+        }
+        const double a = u.area();
+        if (i == 0) root = a;
+        inner += a;
+        const int codes[2] = {nd.child.x, nd.child.y};
+        for (int c = 0; c < 2; ++c)
+            if (codes[c] < 0) {
+                int base, count;
+                leaf_range(codes[c], base, count);
+                leaves += (double)count * cb[c].area();
+            }
+    }
+    return root > 0.0 ? (inner + leaves) / root : 0.0;
 }
 
 }  // namespace dt

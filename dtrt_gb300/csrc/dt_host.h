@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "../../include/dtrt_gb300.h"
+#include "dt_bvh.h"
 #include "dt_kernels.cuh"
 
 namespace dt {
@@ -26,13 +27,28 @@ struct Scratch {
     size_t adj_dimg_n = 0, adj_grad_n = 0, adj_out_n = 0, adj_img_n = 0;
 };
 
+// Connectivity kept from the last build, so that a rebuild from a description with the
+// same triangles (an optimisation step that moves vertices) skips the edge search and
+// refits the BVH instead of building it again.
+struct SceneTopology {
+    bool valid = false;
+    std::vector<int> shape_nv, shape_nt;
+    std::vector<int> indices;                // every shape's triangles, shape-local vertex ids
+    std::vector<int4> adj;                   // per shape: (a, b, f0, f1 or -1), shape-local, sorted by (a, b)
+    std::vector<int> adj_off;                // num_shapes + 1 offsets into adj
+    std::vector<int> media_type, media_res;  // per medium: type; density resolution (3 ints)
+    BvhBuildOut bvh;                         // the tree as last built or refit
+    double sah_build = 0.0;                  // its surface-area cost right after the last full build
+};
+
 }  // namespace dt
 
 struct dtrt_scene {
     int nder = 0;
     int device = 0;
     dt::DevScene dev{};
-    std::vector<void *> allocs;  // scene-lifetime device allocations
+    std::vector<void *> allocs;       // scene-lifetime device allocations, one per upload (null: empty)
+    std::vector<size_t> alloc_bytes;  // byte size of each entry of allocs
     dt::Scratch scratch;
     bool counters = false;
     uint64_t queue_cap = 0;  // 0: automatic
@@ -43,6 +59,7 @@ struct dtrt_scene {
     std::vector<dt::DevMedium> media_host;  // host copy of the device media array
     std::vector<void *> dgrid_bufs;         // per medium: per-voxel derivative directions (owned)
     long long density_voxels = 0;           // voxels of all heterogeneous media (adjoint gradient length)
+    dt::SceneTopology topo;
 };
 
 namespace dt {

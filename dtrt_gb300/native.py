@@ -41,6 +41,16 @@ class NativeScene:
     def __exit__(self, *a):
         self.close()
 
+    def update(self, spec, rebuild_bvh=False):
+        """Rebuild in place from a spec with the same triangles (dtrt_scene_update): the BVH
+        is refit and unchanged-size device arrays are rewritten. Returns the update stats."""
+        desc, keep = spec.to_desc()
+        st = _abi.UpdateStats()
+        _abi.check(self.lib.dtrt_scene_update(self.handle, ctypes.byref(desc),
+                                              _abi.UPDATE_REBUILD_BVH if rebuild_bvh else 0, ctypes.byref(st)))
+        self.spec = spec
+        return st.as_dict()
+
     # ---------------------------------------------------------------- controls
     def set_edge_weights(self, w):
         w = np.ascontiguousarray(w, np.float32)
@@ -172,6 +182,8 @@ class NativeScene:
 
     def trace_closest(self, rays):
         rays = np.ascontiguousarray(rays, np.float32)
+        if rays.ndim != 2 or rays.shape[1] != 8:
+            raise ValueError("rays must be [n][8]: org.xyz, tmin, dir.xyz, tmax")
         n = rays.shape[0]
         hits = np.zeros((n, 2), np.int32)
         t = np.zeros(n, np.float32)

@@ -220,6 +220,34 @@ int dtrt_scene_set_edge_weights(dtrt_scene *scene, const float *weights, int num
 /* Release every device allocation of the scene. */
 int dtrt_scene_destroy(dtrt_scene *scene);
 
+/* In-place rebuild of a scene from a description with the same triangles: the same nder,
+ * number of shapes, per-shape vertex and triangle counts and index lists, the same number
+ * of media with unchanged types and grid resolutions. Everything else (vertex positions,
+ * normals, velocities, camera, materials, emitters, media values, edge weights) is taken
+ * from `desc` as dtrt_scene_create would. What the rebuild reuses instead of recomputing:
+ * the edge adjacency of every mesh, the BVH topology (refit bottom-up to the new positions
+ * while its surface-area cost stays within 2x of its cost when last built, else built
+ * again), and every device array whose size did not change (rewritten in place, so device
+ * pointers stay valid). Kept from the scene: estimator flags, tracking cap, queue capacity,
+ * counters and per-voxel density derivative directions. The reference builds a new scene
+ * for every render (pydtrt/scene_renderer.py:110-316 -> src/scene.cpp:17-43 Embree build,
+ * src/shape.cpp:254-300 edge lists); this replaces that rebuild inside an optimisation loop.
+ * Waits for the device to be idle first (renders in flight may read the arrays). On any
+ * error the scene is unchanged (except a DTRT_ERR_CUDA from the final device copies).
+ * A batch holds a snapshot of its scenes: create it again after an update. */
+#define DTRT_UPDATE_REBUILD_BVH 1u /* build the BVH again instead of refitting it */
+typedef struct dtrt_update_stats {
+    int bvh_refit;         /* 1: refit; 0: built again (flag or surface-area cost past the limit) */
+    int buffers_reused;    /* device arrays rewritten in place */
+    int buffers_allocated; /* device arrays allocated anew (their size changed) */
+    float sah_ratio;       /* surface-area cost of the refit tree / cost at its last full build */
+    double host_ms;        /* wall time of the update, device copies included */
+    double ms_bvh;         /* of which: BVH refit or build */
+    double ms_arrays;      /* of which: every other host array (geometry, edges, tables) */
+    double ms_device;      /* of which: device allocations and copies */
+} dtrt_update_stats;
+int dtrt_scene_update(dtrt_scene *scene, const dtrt_scene_desc *desc, unsigned flags, dtrt_update_stats *stats);
+
 /* Forward-mode render: image plus nder derivative images, float[(nder+1)][H][W][3]
  * row-major (crop size when a crop rectangle is set). `out` is a host pointer when
  * out_on_device == 0, else a device pointer. `stream` is a cudaStream_t or NULL.

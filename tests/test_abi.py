@@ -31,13 +31,14 @@ def test_exports_every_declared_symbol(lib):
 def test_struct_layout_matches_c(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "dtrt_gb300.h"\nint main(void){'
-                   'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dtrt_camera_desc), '
+                   'printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dtrt_camera_desc), '
                    'sizeof(dtrt_shape_desc), sizeof(dtrt_bsdf_desc), sizeof(dtrt_emitter_desc), '
                    'sizeof(dtrt_phase_desc), sizeof(dtrt_medium_desc), sizeof(dtrt_scene_desc), '
                    'sizeof(dtrt_render_options), sizeof(dtrt_render_stats), sizeof(dtrt_batch_item), '
                    'sizeof(dtrt_batch_stats), offsetof(dtrt_medium_desc, to_world), '
                    'offsetof(dtrt_scene_desc, edge_weights), offsetof(dtrt_batch_item, d_image), '
-                   'offsetof(dtrt_batch_stats, item_ms_estimate)); return 0;}\n')
+                   'offsetof(dtrt_batch_stats, item_ms_estimate), sizeof(dtrt_update_stats), '
+                   'offsetof(dtrt_update_stats, ms_device)); return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
@@ -45,7 +46,7 @@ def test_struct_layout_matches_c(tmp_path):
                                        _abi.PhaseDesc, _abi.MediumDesc, _abi.SceneDesc, _abi.RenderOptions,
                                        _abi.RenderStats, _abi.BatchItem, _abi.BatchStats)]
     want += [_abi.MediumDesc.to_world.offset, _abi.SceneDesc.edge_weights.offset, _abi.BatchItem.d_image.offset,
-             _abi.BatchStats.item_ms_estimate.offset]
+             _abi.BatchStats.item_ms_estimate.offset, ctypes.sizeof(_abi.UpdateStats), _abi.UpdateStats.ms_device.offset]
     assert got == want
 
 
@@ -74,6 +75,7 @@ def test_invalid_arguments_are_statuses(lib):
     assert lib.dtrt_scene_create(None, ctypes.byref(h)) == 1
     assert lib.dtrt_render_fwd(None, None, None, 0, None) == 1
     assert lib.dtrt_scene_destroy(None) == 0
+    assert lib.dtrt_scene_update(None, ctypes.byref(desc), 0, None) == 1
 
 
 def test_vol_reader_roundtrip(lib, tmp_path):

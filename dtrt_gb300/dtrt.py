@@ -237,8 +237,26 @@ class Scene:
     device scene (BVH, light and edge distributions) is built here."""
 
     def __init__(self, camera, shapes, bsdfs, emitters, phases, media):
-        from . import scenes as S
         self._nder = camera._nder
+        self.spec = self._spec(camera, shapes, bsdfs, emitters, phases, media)
+        from .native import NativeScene
+        self.native = NativeScene(self.spec)
+
+    def update(self, camera, shapes, bsdfs, emitters, phases, media, rebuild_bvh=False):
+        """Rebuild this scene in place from objects with the same triangles (same shapes,
+        vertex and triangle counts, index lists; same media types and grid sizes): the BVH
+        is refit and the edge adjacency reused (dtrt_scene_update). The reference builds a
+        new Scene for every render instead (scene_renderer.py:313). Returns the update
+        stats; raises DtrtError (status DTRT_ERR_INVALID) when the triangles differ."""
+        if camera._nder != self._nder:
+            raise _abi.DtrtError(_abi.DTRT_ERR_INVALID, "scene update: nder differs from the scene's")
+        spec = self._spec(camera, shapes, bsdfs, emitters, phases, media)
+        st = self.native.update(spec, rebuild_bvh=rebuild_bvh)
+        self.spec = spec
+        return st
+
+    def _spec(self, camera, shapes, bsdfs, emitters, phases, media):
+        from . import scenes as S
         cam = S.CameraSpec(camera.width, camera.height, camera.cam_to_world.reshape(4, 4),
                            camera.cam_to_ndc.reshape(3, 3), camera.clip_near, camera.med_id,
                            camera.velocities.reshape(-1, 3) if camera.velocities is not None else None, camera.rect)
@@ -269,9 +287,7 @@ class Scene:
                                                to_world=m.to_world.reshape(4, 4), density_scale=m.scale,
                                                d_density_scale=m.d_scale, trans_velocities=m.trans_velocities,
                                                rot_velocities=m.rot_velocities))
-        self.spec = spec
-        from .native import NativeScene
-        self.native = NativeScene(spec)
+        return spec
 
     def initEdges(self, weights):
         """Secondary-edge sampling weight per shape (scene.h:37-39)."""

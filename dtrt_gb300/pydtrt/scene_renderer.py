@@ -10,9 +10,16 @@ import time
 
 import torch
 
-from .. import dtrt
+from .. import _abi, dtrt
 
 print_timing = False
+
+# Keep the device scene between render_scene calls and rebuild it in place when the next
+# scene has the same triangles (Scene.update: BVH refit, cached edge adjacency, device
+# arrays rewritten), as in an optimisation loop that moves vertices or changes materials.
+# Off by default: the reference builds a new scene for every call.
+reuse_scene = False
+_kept = None
 
 
 def serialize_scene(scene):
@@ -74,9 +81,10 @@ def _f(x):
     return float(x.reshape(-1)[0]) if torch.is_tensor(x) else float(x)
 
 
-def build_native_scene(*args):
+def build_native_scene(*args, reuse=None):
     """Native objects and the device scene from a flat argument list
-    (scene_renderer.py:110-316). Returns (scene, (H, W))."""
+    (scene_renderer.py:110-316). Returns (scene, (H, W)). With `reuse` (a dtrt.Scene),
+    that scene is updated in place when its triangles match, else a new one is built."""
     num_shapes, num_bsdfs, num_lights, num_medium, num_phases = args[0:5]
     cam_to_world, cam_to_ndc, clip_near, resolution, cam_med_id, cam_vel, rect = args[5:12]
     assert cam_to_world.is_contiguous()
@@ -175,7 +183,16 @@ def build_native_scene(*args):
             i += 3
         else:
             raise ValueError(f"unknown phase type {args[i]!r}")
-    scene = dtrt.Scene(camera, shapes, bsdfs, lights, phases, media)
+    scene = None
+    if reuse is not None and reuse._nder == camera._nder:
+        try:
+            reuse.update(camera, shapes, bsdfs, lights, phases, media)
+            scene = reuse
+        except _abi.DtrtError as e:
+            if e.status != _abi.DTRT_ERR_INVALID:
+                raise
+    if scene is None:
+        scene = dtrt.Scene(camera, shapes, bsdfs, lights, phases, media)
     if args[i] is not None:
         w = args[i].contiguous().float()
         scene.initEdges(dtrt.float_ptr(w.data_ptr()))
@@ -188,11 +205,18 @@ def build_native_scene(*args):
 
 def render_scene(integrator, options, *args):
     """Render the flat-argument scene; returns a float32 CPU tensor (nder+1, H, W, 3)."""
-    scene, (h, w) = build_native_scene(*args)
+    global _kept
+    scene, (h, w) = build_native_scene(*args, reuse=_kept if reuse_scene else None)
+    if _kept is not None and _kept is not scene:
+        _kept.close()
+        _kept = None
     img = torch.zeros(scene._nder + 1, h, w, 3)
     start = time.time()
     integrator.render(scene, options, dtrt.float_ptr(img.data_ptr()))
-    scene.close()
+    if reuse_scene:
+        _kept = scene
+    else:
+        scene.close()
     if print_timing:
         print("Total rendering time: %.2fs" % (time.time() - start))
     return img

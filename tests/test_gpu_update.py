@@ -144,3 +144,28 @@ def test_update_keeps_density_directions_and_flags():
         with pytest.raises(_abi.DtrtError):
             ns.update(other)
         assert np.array_equal(ns.render(seed=9, **kw), before)
+
+
+def test_render_scene_reuse_matches_fresh_builds(monkeypatch):
+    """The pydtrt flat-argument path with reuse_scene on: the second render (vertices
+    scaled) updates the kept scene and renders the same image as a scene built anew."""
+    torch = pytest.importorskip("torch")
+    from test_pydtrt_host import _pydtrt_c2
+    from dtrt_gb300 import dtrt
+    from dtrt_gb300.pydtrt import scene_renderer as sr
+    _, scene = _pydtrt_c2(32, 32)
+    args = sr.serialize_scene(scene)
+    integ = dtrt.VolPathTracerAD()
+    opts = dtrt.RenderOptions(4, 8, 3, 2, 2, True)
+    monkeypatch.setattr(sr, "reuse_scene", True)
+    monkeypatch.setattr(sr, "_kept", None)
+    img1 = sr.render_scene(integ, opts, *args)
+    kept = sr._kept
+    args[12] = (args[12] * 1.05).contiguous()
+    img2 = sr.render_scene(integ, opts, *args)
+    assert sr._kept is kept
+    monkeypatch.setattr(sr, "reuse_scene", False)
+    fresh = sr.render_scene(integ, opts, *args)
+    assert sr._kept is None
+    assert torch.equal(img2, fresh)
+    assert not torch.equal(img1[0], img2[0])

@@ -93,3 +93,56 @@ def test_obj_and_vol_roundtrip(tmp_path):
     scenes.write_vol(str(tmp_path / "g.vol"), g, (0, 0, 0), (1, 1, 1))
     back, vmin, vmax = scenes.read_vol(str(tmp_path / "g.vol"))
     assert np.array_equal(back, g) and vmax == (1.0, 1.0, 1.0)
+
+
+def test_render_scene_reuses_the_device_scene(monkeypatch):
+    """reuse_scene: the second render_scene call with the same triangles updates the kept
+    scene in place; changed triangles build a new scene and close the kept one."""
+    from dtrt_gb300 import _abi
+    from dtrt_gb300.pydtrt import scene_renderer as sr
+
+    class FakeNative:
+        made = []
+
+        def __init__(self, spec):
+            FakeNative.made.append(self)
+            self.spec, self.updates, self.closed = spec, 0, False
+
+        def update(self, spec, rebuild_bvh=False):
+            same = len(spec.shapes) == len(self.spec.shapes) and all(
+                np.array_equal(np.asarray(a.indices), np.asarray(b.indices)) for a, b in zip(spec.shapes, self.spec.shapes))
+            if not same:
+                raise _abi.DtrtError(_abi.DTRT_ERR_INVALID, "scene update: triangles differ")
+            self.spec, self.updates = spec, self.updates + 1
+            return {}
+
+        def set_edge_weights(self, w):
+            pass
+
+        def close(self):
+            self.closed = True
+
+    class Integrator:
+        def render(self, scene, options, image):
+            self.scene = scene
+
+    monkeypatch.setattr(native, "NativeScene", FakeNative)
+    monkeypatch.setattr(sr, "reuse_scene", True)
+    monkeypatch.setattr(sr, "_kept", None)
+    _, scene = _pydtrt_c2()
+    args = sr.serialize_scene(scene)
+    it = Integrator()
+    sr.render_scene(it, None, *args)
+    first = it.scene
+    args[12] = args[12] + 0.01  # vertices of shape 0 move
+    sr.render_scene(it, None, *args)
+    assert it.scene is first and first.native.updates == 1 and len(FakeNative.made) == 1
+    assert np.allclose(np.asarray(first.spec.shapes[0].vertices), np.asarray(args[12]))
+    f = args[13].clone()
+    f[0] = f[0].flip(0)  # one triangle's winding: other triangles
+    args[13] = f
+    sr.render_scene(it, None, *args)
+    assert it.scene is not first and first.native.closed and len(FakeNative.made) == 2
+    monkeypatch.setattr(sr, "reuse_scene", False)
+    sr.render_scene(it, None, *args)  # reuse off: the kept scene is released, the new one closed after use
+    assert FakeNative.made[1].closed and FakeNative.made[2].closed and sr._kept is None

@@ -174,6 +174,7 @@ class BatchStats(ctypes.Structure):
 
 
 UPDATE_REBUILD_BVH = 1
+CAMERA_AUTO, CAMERA_MEGAKERNEL, CAMERA_WAVEFRONT = 0, 1, 2
 
 
 class UpdateStats(ctypes.Structure):
@@ -208,6 +209,7 @@ _SIGNATURES = {
     "dtrt_scene_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderStats)]),
     "dtrt_scene_set_queue_capacity": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "dtrt_scene_set_tracking_cap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dtrt_scene_set_camera_schedule": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dtrt_scene_set_estimator_flags": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint]),
     "dtrt_scene_gradient_sizes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
                                                  ctypes.POINTER(ctypes.c_int64)]),

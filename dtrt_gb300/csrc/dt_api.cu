@@ -999,7 +999,8 @@ void free_scene(dtrt_scene *s) {
         if (p) cudaFree(p);
     s->dgrid_bufs.clear();
     Scratch &b = s->scratch;
-    void *ptrs[] = {b.acc1, b.acc2, b.out, b.qe, b.ql, b.qli, b.counts, b.err, b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img};
+    void *ptrs[] = {b.acc1,     b.acc2,     b.out,     b.qe,     b.ql,      b.qli,       b.counts,   b.err,
+                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     b = Scratch();
@@ -1204,6 +1205,15 @@ int dtrt_scene_last_stats(const dtrt_scene *scene, dtrt_render_stats *out) {
 int dtrt_scene_set_queue_capacity(dtrt_scene *scene, uint64_t max_tasks) {
     if (!scene) return DTRT_ERR_INVALID;
     scene->queue_cap = max_tasks;
+    return DTRT_OK;
+}
+
+int dtrt_scene_set_camera_schedule(dtrt_scene *scene, int schedule) {
+    if (!scene || schedule < DTRT_CAMERA_AUTO || schedule > DTRT_CAMERA_WAVEFRONT) {
+        dt::set_last_error("unknown camera schedule");
+        return DTRT_ERR_INVALID;
+    }
+    scene->camera_schedule = schedule;
     return DTRT_OK;
 }
 

@@ -25,6 +25,9 @@ struct Scratch {
     float *adj_dimg = nullptr, *adj_grad = nullptr, *adj_out = nullptr;
     double *adj_img = nullptr;
     size_t adj_dimg_n = 0, adj_grad_n = 0, adj_out_n = 0, adj_img_n = 0;
+    // wavefront camera schedule: per-path state, two path-index queues, per-level counts
+    void *cam_state = nullptr, *cam_q = nullptr, *cam_cnt = nullptr;
+    size_t cam_state_bytes = 0, cam_q_bytes = 0, cam_cnt_bytes = 0;
 };
 
 // Connectivity kept from the last build, so that a rebuild from a description with the
@@ -52,6 +55,7 @@ struct dtrt_scene {
     dt::Scratch scratch;
     bool counters = false;
     uint64_t queue_cap = 0;  // 0: automatic
+    int camera_schedule = 0;  // DTRT_CAMERA_AUTO / _MEGAKERNEL / _WAVEFRONT
     dtrt_render_stats last{};
     int num_shapes = 0;
     std::vector<float> shape_edge_len;  // per shape total edge length (for re-weighting)

@@ -142,188 +142,208 @@ DT_D RayAD<N> camera_ray_ad(const DevCamera &cam, double x, double y) {
 }
 
 // ====================================================================== camera AD paths
+// State of one camera path between vertices (volpathAD.cpp:145-620 as a loop): the
+// megakernel keeps it in registers, the wavefront schedule in HBM between launches.
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_camera(DevScene sc, RenderParams rp, Queue qe, Queue ql, double *acc1,
-                                                   unsigned long long *ctr) {
-    __shared__ int s_stack[kStackDepth * kBlock];
-    int *stack = s_stack + threadIdx.x;
-    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
-    const bool active = gi < rp.path_count;
-    const long long g = rp.path_begin + (active ? gi : 0);
+struct CamState {
+    Rng rng;
+    RayAD<N> ray;
+    ItsAD<N> its;
+    DV<N> P, acc;
+    int med, depth, mode, level;
+};
+
+// Path start: jittered primary ray and first intersection. False: nothing was hit.
+template <int N>
+DT_D bool camera_start(const DevScene &sc, const RenderParams &rp, int *stack, long long g, CamState<N> &st, Ctr &c) {
     const int pixel = (int)(g / rp.spp);
-    const int sample = (int)(g % rp.spp);
-    Ctr c;
-    DV<N> acc;
-    if (active) {
-        const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
-        const uint64_t key = (uint64_t)g;
-        Rng rng;
-        rng.init(rp.seed, key);
-        double jx = 0.5, jy = 0.5;
-        if (rp.jitter) {
-            jx = rng.next1d();
-            jy = rng.next1d();
-        }
-        RayAD<N> ray = camera_ray_ad<N>(sc.cam, ix + jx, iy + jy);
-        ItsAD<N> its;
-        int med = sc.cam.med_id;
-        int depth = rp.max_bounces;
-        int mode = rp.mode;
-        DV<N> P(mk(1.f, 1.f, 1.f));
-        bool alive = ray_intersect_ad<N>(sc, stack, ray, false, its, c);
-        for (int level = 0; alive && mode != 0; ++level) {
-            alive = false;
-            const float r1a = rng.next1(), r1b = rng.next1();
-            float r2[4];
-            r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
-            const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
-            DV<N> thr(mk(1.f, 1.f, 1.f));
-            const float3 dir_in = ray.d.val();
-            if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c)) {
-                // ------------------------------------------------ volumetric vertex, volpathAD.cpp:164-305
-                if (depth == 0 || thr.is_zero()) break;
-                const DevPhase &ph = sc.phases[sc.media[med].phase_id];
-                const DV<N> Q = cmul(P, thr);
-                DV<N> wo;
-                float pdf_nee;
-                if (mode & MODE_VOLUME_MAIN) {
-                    DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
-                    if (!v.is_zero()) {
-                        Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
-                        if (pv.v > kEps) acc += cmul(Q, v) * (pv * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
-                    }
-                }
-                // edge record before the continuation overwrites the vertex state
-                if (rp.sppse > 0 && (mode & MODE_VOLUME_BOUNDARY2) && sc.has_edges &&
-                    (sc.moving_geometry || !ray.o.der_zero(0.f))) {
-                    const long long slot = queue_reserve(sc, qe);
-                    if (slot >= 0) {
-                        EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
-                        const float3 x = ray.o.val(), w = cmul(P.val(), thr.val()) * rp.inv_spp, wi = -dir_in;
-                        r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
-#pragma unroll
-                        for (int j = 0; j < N; ++j) {
-                            const float3 gj = ray.o.grad(j);
-                            r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
-                        }
-                        r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
-                        r.wi[0] = wi.x; r.wi[1] = wi.y; r.wi[2] = wi.z;
-                        r.kind = 1; r.shape = -1; r.med = med; r.phase = sc.media[med].phase_id;
-                        r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 1u, (uint32_t)level);
-                    }
-                }
-                const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
-                if (pvs.v > kEps) {
-                    const DV<N> thr1 = thr * pvs;
-                    ray.d = wo;
-                    ItsAD<N> its1;
-                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
-                                                       nullptr, c);
-                    if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
-                        acc += cmul(cmul(P, thr1), att) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
-                    its = its1;
-                    P = cmul(P, thr1);
-                    depth -= 1;
-                    mode &= ~MODE_EMISSION;
-                    alive = true;
-                }
-                continue;
-            }
-            // ---------------------------------------------------- interface vertex, volpathAD.cpp:306-617
-            if (!its.valid() || thr.is_zero()) break;
-            const DevShape &sh = sc.shapes[its.shape];
-            if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) break;
-            const DV<N> Q = cmul(P, thr);
-            if (sh.light_id >= 0 && (mode & MODE_EMISSION)) acc += cmul(Q, le_ad<N>(sc, its, -ray.d));
-            if (depth == 0) break;
-            const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
-            const bool is_null = b.type == BSDF_NULL;
-            const FrameAD<N> fr = its.frame();
-            const Its its0 = its.plain();
-            // Lins boundary term, volpathAD.cpp:321-467
-            if (med >= 0 && !its.t.der_zero(kDerZeroEps) && (mode & MODE_VOLUME_BOUNDARY1)) {
-                const long long slot = queue_reserve(sc, ql);
-                if (slot >= 0) {
-                    LinsRec<N> &r = reinterpret_cast<LinsRec<N> *>(ql.data)[slot];
-                    float3 n = its0.ng;
-                    if (dot(n, dir_in) < 0.f) n = -n;
-                    const int ns = min(max((int)(rp.ddist * its.t.der_max()), 1), 100);
-                    const float3 sig = sig_s(sc.media[med], its0.p - n * kShadowEps, c);
-                    const float3 w = cmul(cmul(P.val(), thr.val()), sig) * (rp.inv_spp / (float)ns);
-                    const float3 *src[8] = {&its0.p, &its0.ng, &n, &dir_in, &its0.fr.s, &its0.fr.t, &its0.fr.n, &its0.wi};
-                    float *dst[8] = {r.p, r.ng, r.n, r.rd, r.fs, r.ft, r.fn, r.wi};
-                    for (int k = 0; k < 8; ++k) { dst[k][0] = src[k]->x; dst[k][1] = src[k]->y; dst[k][2] = src[k]->z; }
-                    r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
-#pragma unroll
-                    for (int j = 0; j < N; ++j) r.s[j] = its.t.d[j];
-                    r.shape = its.shape; r.med = med; r.phase = sc.media[med].phase_id; r.depth = depth;
-                    r.pixel = pixel; r.ns = ns; r.key = child_key(key, 2u, (uint32_t)level);
-                }
-            }
-            // interface edge record, volpathAD.cpp:513-616
-            if (!is_null && rp.sppse > 0 && (mode & MODE_SURFACE_BOUNDARY) && sc.has_edges &&
-                (sc.moving_geometry || !its.p.der_zero(0.f))) {
-                const long long slot = queue_reserve(sc, qe);
-                if (slot >= 0) {
-                    EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
-                    const float3 x = its0.p, w = cmul(P.val(), thr.val()) * rp.inv_spp;
-                    r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
-#pragma unroll
-                    for (int j = 0; j < N; ++j) {
-                        const float3 gj = its.p.grad(j);
-                        r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
-                    }
-                    r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
-                    r.wi[0] = its0.wi.x; r.wi[1] = its0.wi.y; r.wi[2] = its0.wi.z;
-                    r.fs[0] = its0.fr.s.x; r.fs[1] = its0.fr.s.y; r.fs[2] = its0.fr.s.z;
-                    r.ft[0] = its0.fr.t.x; r.ft[1] = its0.fr.t.y; r.ft[2] = its0.fr.t.z;
-                    r.fn[0] = its0.fr.n.x; r.fn[1] = its0.fr.n.y; r.fn[2] = its0.fr.n.z;
-                    r.ng[0] = its0.ng.x; r.ng[1] = its0.ng.y; r.ng[2] = its0.ng.z;
-                    r.kind = 0; r.shape = its.shape; r.med = med; r.phase = -1;
-                    r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 3u, (uint32_t)level);
-                }
-            }
-            // area sampling, volpathAD.cpp:469-511
-            DV<N> wo;
-            float pdf_nee;
-            if (!is_null && (mode & MODE_SURFACE_MAIN)) {
-                DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
-                if (!v.is_zero()) {
-                    const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
-                    const float bp = bsdf_pdf(b, its0.wi, wo.val());
-                    acc += cmul(cmul(Q, v), bv) * mis_weight(pdf_nee, bp);
-                }
-            }
-            float bpdf, beta;
-            const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
-            if (!bw.is_zero()) {
-                wo = fr.to_world(wo);
-                if (!is_null) wo = zero_grad(wo);  // asserted zero in the reference (volpathAD.cpp:489)
-                ray.o = its.p;
-                ray.d = wo;
-                const int med1 = is_transition(sh) ? target_medium(sc, its.shape, its.ng, wo.val()) : med;
-                DV<N> thr1 = thr;
-                ItsAD<N> its1;
-                if (is_null) {
-                    ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
-                } else {
-                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee,
-                                                       nullptr, nullptr, c);
-                    thr1 = cmul(thr1, bw);
-                    if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
-                        acc += cmul(cmul(P, thr1), att) * mis_weight(bpdf, pdf_nee);
-                    mode &= ~MODE_EMISSION;
-                }
-                its = its1;
-                P = cmul(P, thr1);
-                med = med1;
-                depth -= 1;
-                alive = true;
-            }
-        }
-        acc = acc * rp.inv_spp;
+    const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
+    st.rng.init(rp.seed, (uint64_t)g);
+    double jx = 0.5, jy = 0.5;
+    if (rp.jitter) {
+        jx = st.rng.next1d();
+        jy = st.rng.next1d();
     }
-    // accumulate: a warp whose 32 lanes share one pixel reduces with shuffles first
+    st.ray = camera_ray_ad<N>(sc.cam, ix + jx, iy + jy);
+    st.its = ItsAD<N>();
+    st.med = sc.cam.med_id;
+    st.depth = rp.max_bounces;
+    st.mode = rp.mode;
+    st.level = 0;
+    st.P = DV<N>(mk(1.f, 1.f, 1.f));
+    st.acc = DV<N>();
+    return ray_intersect_ad<N>(sc, stack, st.ray, false, st.its, c);
+}
+
+// One vertex of camera path g: a volume vertex (NEE, volume edge record, phase sampling)
+// or an interface vertex (emission, Lins and surface edge records, NEE, BSDF sampling).
+// Returns whether the path continues; st.level is advanced by the caller.
+template <int N>
+DT_D bool camera_step(const DevScene &sc, const RenderParams &rp, int *stack, long long g, CamState<N> &st,
+                      const Queue &qe, const Queue &ql, Ctr &c) {
+    Rng &rng = st.rng;
+    RayAD<N> &ray = st.ray;
+    ItsAD<N> &its = st.its;
+    DV<N> &P = st.P, &acc = st.acc;
+    int &med = st.med, &depth = st.depth, &mode = st.mode;
+    const int level = st.level;
+    const int pixel = (int)(g / rp.spp);
+    const uint64_t key = (uint64_t)g;
+    bool alive = false;
+    const float r1a = rng.next1(), r1b = rng.next1();
+    float r2[4];
+    r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
+    const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
+    DV<N> thr(mk(1.f, 1.f, 1.f));
+    const float3 dir_in = ray.d.val();
+    if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c)) {
+        // ------------------------------------------------ volumetric vertex, volpathAD.cpp:164-305
+        if (depth == 0 || thr.is_zero()) return false;
+        const DevPhase &ph = sc.phases[sc.media[med].phase_id];
+        const DV<N> Q = cmul(P, thr);
+        DV<N> wo;
+        float pdf_nee;
+        if (mode & MODE_VOLUME_MAIN) {
+            DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
+            if (!v.is_zero()) {
+                Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+                if (pv.v > kEps) acc += cmul(Q, v) * (pv * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
+            }
+        }
+        // edge record before the continuation overwrites the vertex state
+        if (rp.sppse > 0 && (mode & MODE_VOLUME_BOUNDARY2) && sc.has_edges &&
+            (sc.moving_geometry || !ray.o.der_zero(0.f))) {
+            const long long slot = queue_reserve(sc, qe);
+            if (slot >= 0) {
+                EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
+                const float3 x = ray.o.val(), w = cmul(P.val(), thr.val()) * rp.inv_spp, wi = -dir_in;
+                r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const float3 gj = ray.o.grad(j);
+                    r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
+                }
+                r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+                r.wi[0] = wi.x; r.wi[1] = wi.y; r.wi[2] = wi.z;
+                r.kind = 1; r.shape = -1; r.med = med; r.phase = sc.media[med].phase_id;
+                r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 1u, (uint32_t)level);
+            }
+        }
+        const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
+        if (pvs.v > kEps) {
+            const DV<N> thr1 = thr * pvs;
+            ray.d = wo;
+            ItsAD<N> its1;
+            DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
+                                               nullptr, c);
+            if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+                acc += cmul(cmul(P, thr1), att) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+            its = its1;
+            P = cmul(P, thr1);
+            depth -= 1;
+            mode &= ~MODE_EMISSION;
+            alive = true;
+        }
+        return alive;
+    }
+    // ---------------------------------------------------- interface vertex, volpathAD.cpp:306-617
+    if (!its.valid() || thr.is_zero()) return false;
+    const DevShape &sh = sc.shapes[its.shape];
+    if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) return false;
+    const DV<N> Q = cmul(P, thr);
+    if (sh.light_id >= 0 && (mode & MODE_EMISSION)) acc += cmul(Q, le_ad<N>(sc, its, -ray.d));
+    if (depth == 0) return false;
+    const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
+    const bool is_null = b.type == BSDF_NULL;
+    const FrameAD<N> fr = its.frame();
+    const Its its0 = its.plain();
+    // Lins boundary term, volpathAD.cpp:321-467
+    if (med >= 0 && !its.t.der_zero(kDerZeroEps) && (mode & MODE_VOLUME_BOUNDARY1)) {
+        const long long slot = queue_reserve(sc, ql);
+        if (slot >= 0) {
+            LinsRec<N> &r = reinterpret_cast<LinsRec<N> *>(ql.data)[slot];
+            float3 n = its0.ng;
+            if (dot(n, dir_in) < 0.f) n = -n;
+            const int ns = min(max((int)(rp.ddist * its.t.der_max()), 1), 100);
+            const float3 sig = sig_s(sc.media[med], its0.p - n * kShadowEps, c);
+            const float3 w = cmul(cmul(P.val(), thr.val()), sig) * (rp.inv_spp / (float)ns);
+            const float3 *src[8] = {&its0.p, &its0.ng, &n, &dir_in, &its0.fr.s, &its0.fr.t, &its0.fr.n, &its0.wi};
+            float *dst[8] = {r.p, r.ng, r.n, r.rd, r.fs, r.ft, r.fn, r.wi};
+            for (int k = 0; k < 8; ++k) { dst[k][0] = src[k]->x; dst[k][1] = src[k]->y; dst[k][2] = src[k]->z; }
+            r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+#pragma unroll
+            for (int j = 0; j < N; ++j) r.s[j] = its.t.d[j];
+            r.shape = its.shape; r.med = med; r.phase = sc.media[med].phase_id; r.depth = depth;
+            r.pixel = pixel; r.ns = ns; r.key = child_key(key, 2u, (uint32_t)level);
+        }
+    }
+    // interface edge record, volpathAD.cpp:513-616
+    if (!is_null && rp.sppse > 0 && (mode & MODE_SURFACE_BOUNDARY) && sc.has_edges &&
+        (sc.moving_geometry || !its.p.der_zero(0.f))) {
+        const long long slot = queue_reserve(sc, qe);
+        if (slot >= 0) {
+            EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
+            const float3 x = its0.p, w = cmul(P.val(), thr.val()) * rp.inv_spp;
+            r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const float3 gj = its.p.grad(j);
+                r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
+            }
+            r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+            r.wi[0] = its0.wi.x; r.wi[1] = its0.wi.y; r.wi[2] = its0.wi.z;
+            r.fs[0] = its0.fr.s.x; r.fs[1] = its0.fr.s.y; r.fs[2] = its0.fr.s.z;
+            r.ft[0] = its0.fr.t.x; r.ft[1] = its0.fr.t.y; r.ft[2] = its0.fr.t.z;
+            r.fn[0] = its0.fr.n.x; r.fn[1] = its0.fr.n.y; r.fn[2] = its0.fr.n.z;
+            r.ng[0] = its0.ng.x; r.ng[1] = its0.ng.y; r.ng[2] = its0.ng.z;
+            r.kind = 0; r.shape = its.shape; r.med = med; r.phase = -1;
+            r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 3u, (uint32_t)level);
+        }
+    }
+    // area sampling, volpathAD.cpp:469-511
+    DV<N> wo;
+    float pdf_nee;
+    if (!is_null && (mode & MODE_SURFACE_MAIN)) {
+        DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+        if (!v.is_zero()) {
+            const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
+            const float bp = bsdf_pdf(b, its0.wi, wo.val());
+            acc += cmul(cmul(Q, v), bv) * mis_weight(pdf_nee, bp);
+        }
+    }
+    float bpdf, beta;
+    const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
+    if (!bw.is_zero()) {
+        wo = fr.to_world(wo);
+        if (!is_null) wo = zero_grad(wo);  // asserted zero in the reference (volpathAD.cpp:489)
+        ray.o = its.p;
+        ray.d = wo;
+        const int med1 = is_transition(sh) ? target_medium(sc, its.shape, its.ng, wo.val()) : med;
+        DV<N> thr1 = thr;
+        ItsAD<N> its1;
+        if (is_null) {
+            ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
+        } else {
+            DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee,
+                                               nullptr, nullptr, c);
+            thr1 = cmul(thr1, bw);
+            if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
+                acc += cmul(cmul(P, thr1), att) * mis_weight(bpdf, pdf_nee);
+            mode &= ~MODE_EMISSION;
+        }
+        its = its1;
+        P = cmul(P, thr1);
+        med = med1;
+        depth -= 1;
+        alive = true;
+    }
+    return alive;
+}
+
+// FP64 pixel accumulation of a path's contribution (already divided by spp): a warp
+// whose 32 lanes share one pixel reduces with shuffles first. Every lane of the warp calls it.
+template <int N>
+DT_D void accumulate_path(const RenderParams &rp, bool active, int pixel, const DV<N> &acc, double *acc1) {
     const unsigned full = 0xffffffffu;
     const int p0 = __shfl_sync(full, pixel, 0);
     const bool uniform = __all_sync(full, active && pixel == p0);
@@ -349,7 +369,90 @@ __global__ void __launch_bounds__(kBlock) k_camera(DevScene sc, RenderParams rp,
             if (vals[k] != 0.f) atomicAdd(acc1 + ((size_t)(k / 3) * rp.npix + pixel) * 3 + (k % 3), (double)vals[k]);
         }
     }
+}
+
+// Megakernel schedule: one thread runs its camera path to the end.
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_camera(DevScene sc, RenderParams rp, Queue qe, Queue ql, double *acc1,
+                                                   unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < rp.path_count;
+    const long long g = rp.path_begin + (active ? gi : 0);
+    Ctr c;
+    DV<N> acc;
+    if (active) {
+        CamState<N> st;
+        bool alive = camera_start<N>(sc, rp, stack, g, st, c);
+        while (alive && st.mode != 0) {
+            alive = camera_step<N>(sc, rp, stack, g, st, qe, ql, c);
+            ++st.level;
+        }
+        acc = st.acc * rp.inv_spp;
+    }
+    accumulate_path<N>(rp, active, (int)(g / rp.spp), acc, acc1);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// Wavefront schedule: paths that continue are compacted into a queue of path indices
+// after every vertex, so each launch runs one vertex of live paths only (a warp no longer
+// idles on the paths of its lanes that ended early).
+DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = id;  // at most one push per path and level
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams rp, CamState<N> *states, int *q_out,
+                                                      unsigned long long *cnt_out, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    bool live = false;
+    if (gi < rp.path_count) {
+        CamState<N> st;
+        live = camera_start<N>(sc, rp, stack, rp.path_begin + gi, st, c) && st.mode != 0;
+        states[gi] = st;
+    }
+    push_path(q_out, cnt_out, (int)gi, live);
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_cam_level(DevScene sc, RenderParams rp, CamState<N> *states, const int *q_in,
+                                                      const unsigned long long *cnt_in, int *q_out,
+                                                      unsigned long long *cnt_out, Queue qe, Queue ql,
+                                                      unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long n = (long long)*cnt_in;
+    Ctr c;
+    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
+        const int id = q_in[i];
+        CamState<N> st = states[id];
+        const bool alive = camera_step<N>(sc, rp, stack, rp.path_begin + id, st, qe, ql, c);
+        ++st.level;
+        states[id] = st;
+        push_path(q_out, cnt_out, id, alive && st.mode != 0);
+    }
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_cam_accum(RenderParams rp, const CamState<N> *states, double *acc1) {
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < rp.path_count;
+    DV<N> acc;
+    if (active) acc = states[gi].acc * rp.inv_spp;
+    accumulate_path<N>(rp, active, (int)((rp.path_begin + (active ? gi : 0)) / rp.spp), acc, acc1);
 }
 
 // ====================================================================== FP64 edge geometry

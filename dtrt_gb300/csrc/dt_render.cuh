@@ -27,6 +27,9 @@ namespace dt {
         }                                                                            \
     } while (0)
 
+// AUTO camera schedule: the wavefront from this many paths per batch
+constexpr long long kWavefrontMinPaths = 1 << 16;
+
 template <int N>
 int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t st) {
     using clk = std::chrono::steady_clock;
@@ -126,15 +129,46 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         long long B = (long long)(rec_cap / (uint64_t)std::max(1, o->max_bounces + 1));
         B = std::max<long long>(unit, (B / unit) * unit);
         const long long per_chunk = std::max<long long>(1, (long long)(li_cap / (uint64_t)std::max(1, 2 * rp.sppse)));
+        // camera schedule: the wavefront keeps CamState per path of a batch in device memory
+        const long long Bw = std::min<long long>(B, total);
+        const int levels = o->max_bounces + 1;  // a continuing vertex always spends one bounce
+        bool wavefront = s->camera_schedule == DTRT_CAMERA_WAVEFRONT ||
+                         (s->camera_schedule == DTRT_CAMERA_AUTO && Bw >= kWavefrontMinPaths);
+        if (wavefront && !(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, (size_t)Bw * sizeof(CamState<N>)) &&
+                           ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)2 * Bw * sizeof(int)) &&
+                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)(levels + 1) * sizeof(unsigned long long)))) {
+            if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
+            cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
+            wavefront = false;
+        }
+        int sms = 0;
+        DT_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+        CamState<N> *states = (CamState<N> *)sb.cam_state;
+        int *qa = (int *)sb.cam_q, *qb = qa + Bw;
+        unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt;
         for (long long b0 = 0; b0 < total; b0 += B) {
             ++batches;
             rp.path_begin = b0;
             rp.path_count = std::min(B, total - b0);
             DT_CK(cudaMemsetAsync(sb.counts, 0, 3 * sizeof(unsigned long long), st));
-            if ((rc = timed(ms_camera, [&] {
-                     k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
-                 })))
+            if (wavefront) {
+                // grid-stride launches of a few waves: late levels hold few live paths
+                const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
+                if ((rc = timed(ms_camera, [&] {
+                         cudaMemsetAsync(lcnt, 0, (size_t)(levels + 1) * sizeof(unsigned long long), st);
+                         k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, lcnt, ctr);
+                         for (int L = 0; L < levels; ++L)
+                             k_cam_level<N><<<gw, kBlock, 0, st>>>(sc, rp, states, (L & 1) ? qb : qa, lcnt + L,
+                                                                   (L & 1) ? qa : qb, lcnt + L + 1, qe, ql, ctr);
+                         k_cam_accum<N><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, sb.acc1);
+                     })))
+                    return rc;
+                launches += levels + 1;
+            } else if ((rc = timed(ms_camera, [&] {
+                            k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
+                        }))) {
                 return rc;
+            }
             if ((rc = read_counts())) return rc;
             const unsigned long long ne = std::min<unsigned long long>(hcnt[0], rec_cap);
             const unsigned long long nl = std::min<unsigned long long>(hcnt[1], rec_cap);

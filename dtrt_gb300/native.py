@@ -62,6 +62,12 @@ class NativeScene:
     def set_queue_capacity(self, n):
         _abi.check(self.lib.dtrt_scene_set_queue_capacity(self.handle, int(n)))
 
+    def set_camera_schedule(self, schedule):
+        """'auto', 'megakernel' or 'wavefront' (dtrt_scene_set_camera_schedule)."""
+        v = {"auto": _abi.CAMERA_AUTO, "megakernel": _abi.CAMERA_MEGAKERNEL, "wavefront": _abi.CAMERA_WAVEFRONT}
+        _abi.check(self.lib.dtrt_scene_set_camera_schedule(self.handle, v[schedule] if isinstance(schedule, str)
+                                                           else int(schedule)))
+
     def set_tracking_cap(self, n):
         _abi.check(self.lib.dtrt_scene_set_tracking_cap(self.handle, int(n)))
 

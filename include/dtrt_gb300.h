@@ -302,6 +302,17 @@ int dtrt_scene_set_queue_capacity(dtrt_scene *scene, uint64_t max_tasks);
  * returns DTRT_ERR_STEP_CAP. */
 int dtrt_scene_set_tracking_cap(dtrt_scene *scene, int max_steps);
 
+/* How forward-mode renders run the camera paths of pass 1 (integratorAD.cpp:19-98):
+ * MEGAKERNEL: one thread carries its path to the end in one launch; WAVEFRONT: one launch
+ * per path vertex over the paths still alive, compacted into a queue after every vertex
+ * (path state in device memory between launches); AUTO picks per render. Same estimator,
+ * same random numbers per path: the images agree up to FP32 rounding and the order of
+ * the FP64 pixel sums. dtrt_render_fwd_noalloc always uses the megakernel. */
+#define DTRT_CAMERA_AUTO 0
+#define DTRT_CAMERA_MEGAKERNEL 1
+#define DTRT_CAMERA_WAVEFRONT 2
+int dtrt_scene_set_camera_schedule(dtrt_scene *scene, int schedule);
+
 /* ---------------------------------------------------------------- reverse mode and density
  * parameters. None of these has a counterpart in the reference: its heterogeneous medium
  * differentiates the lookup position, the density scale and the albedo only

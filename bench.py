@@ -264,8 +264,11 @@ def run_gpu(args, wl_name, rank, world, local_rank):
         t = json.load(open(tfile)).get(f"{wl_name}:{dom}")
         if t:
             traffic = t["dram_bytes_per_path"] * paths_per_step
+    kname = f"k_{dom}"
+    if dom == "camera" and cstats.get("camera_schedule") == 2:
+        kname = "k_cam_level (camera stage: k_cam_start + one k_cam_level per vertex + k_cam_accum)"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": f"k_{dom}",
+                "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": kname,
                 "peak_source": "measured" if peaks else "fallback",
                 "bytes_per_step": alg_bytes,
                 "bytes_model": "64 B per BVH node visit + 48 B per triangle test + 32 B per trilinear lookup "

@@ -123,7 +123,7 @@ class RenderStats(ctypes.Structure):
         ("k_tri_tests", ctypes.c_uint64 * 5), ("k_grid_lookups", ctypes.c_uint64 * 5),
         ("ms_total", ctypes.c_double), ("ms_camera", ctypes.c_double), ("ms_edge", ctypes.c_double),
         ("ms_li", ctypes.c_double), ("ms_primary", ctypes.c_double), ("ms_setup", ctypes.c_double),
-        ("counters_enabled", ctypes.c_int),
+        ("counters_enabled", ctypes.c_int), ("camera_schedule", ctypes.c_int),
     ]
 
     def as_dict(self):

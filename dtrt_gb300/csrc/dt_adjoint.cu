@@ -108,12 +108,53 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     uint64_t launches = 0;
     float ms_replay = 0.f;
     DT_ACK(cudaEventRecord(e0, st));
-    const long long B = 1ll << 24;  // paths per launch
+    // schedule: the wavefront (pass A and pass B each one launch per vertex over the live
+    // paths) for large renders, as dtrt_render_fwd's camera schedule
+    long long B = 1ll << 24;  // paths per launch (megakernel) or per wavefront chunk
+    bool wavefront = s->camera_schedule == DTRT_CAMERA_WAVEFRONT ||
+                     (s->camera_schedule == DTRT_CAMERA_AUTO && total >= kWavefrontMinPaths);
+    const int levels = o->max_bounces + 1;
+    if (wavefront) {
+        B = std::min<long long>(1ll << 22, std::max<long long>(total, 1));
+        if (!(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, (size_t)B * sizeof(AdjState<1>)) &&
+              ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)2 * B * sizeof(int)) &&
+              ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)2 * (levels + 1) * sizeof(unsigned long long)) &&
+              ensure_buffer(&sb.adj_tot, &sb.adj_tot_bytes, (size_t)B * sizeof(float3)) &&
+              ensure_buffer(&sb.adj_ev, &sb.adj_ev_bytes, (size_t)B * kReplayEvents * sizeof(float3)))) {
+            if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
+            cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
+            wavefront = false;
+            B = 1ll << 24;
+        }
+    }
+    int sms = 0;
+    DT_ACK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+    AdjState<1> *states = (AdjState<1> *)sb.cam_state;
+    int *qa = (int *)sb.cam_q, *qb = qa + B;
+    unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt;
+    float3 *tots = (float3 *)sb.adj_tot, *evb = (float3 *)sb.adj_ev;
+    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
     for (long long b0 = 0; b0 < total; b0 += B) {
         rp.path_begin = b0;
         rp.path_count = std::min(B, total - b0);
-        DT_ACK(launch_adjoint(sc, rp, dimg, grad, img_acc, ctr, 1, st));
-        ++launches;
+        if (!wavefront) {
+            DT_ACK(launch_adjoint(sc, rp, dimg, grad, img_acc, ctr, 1, st));
+            ++launches;
+            continue;
+        }
+        const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
+        const bool pass_b = grad != nullptr && dimg != nullptr;
+        DT_ACK(cudaMemsetAsync(lcnt, 0, (size_t)2 * (levels + 1) * sizeof(unsigned long long), st));
+        for (int pass = 0; pass < (pass_b ? 2 : 1); ++pass) {
+            unsigned long long *cnt = lcnt + pass * (levels + 1);
+            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, cnt, dimg, tots, pass == 1, ctr);
+            for (int L = 0; L < levels; ++L)
+                k_adj_level<1><<<gw, kBlock, 0, st>>>(sc, rp, states, (L & 1) ? qb : qa, cnt + L, (L & 1) ? qa : qb,
+                                                     cnt + L + 1, dimg, grad, tots, evb, pass == 1, ctr);
+            if (pass == 0) k_adj_totals<1><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, tots, img_acc);
+            launches += levels + 1 + (pass == 0 ? 1 : 0);
+        }
+        DT_ACK(cudaGetLastError());
     }
     DT_ACK(cudaEventRecord(e1, st));
     if (image) {
@@ -142,6 +183,7 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     ls.kernel_launches = launches;
     ls.batches = (uint64_t)((total + B - 1) / B);
     ls.counters_enabled = ctr != nullptr;
+    ls.camera_schedule = wavefront ? DTRT_CAMERA_WAVEFRONT : DTRT_CAMERA_MEGAKERNEL;
     ls.k_rays[0] = ls.rays = hc[0];
     ls.k_node_visits[0] = ls.node_visits = hc[1];
     ls.k_tri_tests[0] = ls.tri_tests = hc[2];

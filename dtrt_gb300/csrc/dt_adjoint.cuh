@@ -36,142 +36,82 @@ namespace dt {
 // the rewind of the RNG state instead.
 constexpr int kReplayEvents = 40;
 
+// State of one replayed camera path between vertices (wavefront schedule: in HBM).
 template <int N>
-DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, long long g, int pixel, bool pass_b,
-                        float3 total, float3 gpix, AdjCtx &adj, Ctr &c, float3 *ev) {
-    int ne = 0;  // event index, in path order (identical in both passes)
-    const float3 zero = mk(0.f, 0.f, 0.f);
-    const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
+struct AdjState {
     Rng rng;
-    rng.init(rp.seed, (uint64_t)g);
+    RayAD<N> ray;
+    ItsAD<N> its;
+    float3 P, acc;
+    int med, depth, mode, level, ne;  // ne: event index, in path order (identical in both passes)
+};
+
+template <int N>
+DT_D bool replay_start(const DevScene &sc, const RenderParams &rp, int *stack, long long g, AdjState<N> &st, Ctr &c) {
+    const int pixel = (int)(g / rp.spp);
+    const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
+    st.rng.init(rp.seed, (uint64_t)g);
     double jx = 0.5, jy = 0.5;
     if (rp.jitter) {
-        jx = rng.next1d();
-        jy = rng.next1d();
+        jx = st.rng.next1d();
+        jy = st.rng.next1d();
     }
-    RayAD<N> ray = camera_ray_ad<N>(sc.cam, ix + jx, iy + jy);
-    ItsAD<N> its;
-    int med = sc.cam.med_id;
-    int depth = rp.max_bounces;
-    int mode = rp.mode;
-    float3 P = mk(1.f, 1.f, 1.f), acc = zero;
+    st.ray = camera_ray_ad<N>(sc.cam, ix + jx, iy + jy);
+    st.its = ItsAD<N>();
+    st.med = sc.cam.med_id;
+    st.depth = rp.max_bounces;
+    st.mode = rp.mode;
+    st.level = 0;
+    st.ne = 0;
+    st.P = mk(1.f, 1.f, 1.f);
+    st.acc = mk(0.f, 0.f, 0.f);
+    return ray_intersect_ad<N>(sc, stack, st.ray, false, st.its, c);
+}
+
+// One vertex of the replayed path (camera_step's branches, values only). Pass B scatters
+// dot(dL/dI, suffix)/spp into the voxels behind every distance-sampling factor and each
+// NEE / emitter-hit event's own weight; ev holds pass A's event values.
+template <int N>
+DT_D bool replay_step(const DevScene &sc, const RenderParams &rp, int *stack, bool pass_b, float3 total, float3 gpix,
+                      AdjCtx &adj, Ctr &c, float3 *ev, AdjState<N> &st) {
+    Rng &rng = st.rng;
+    RayAD<N> &ray = st.ray;
+    ItsAD<N> &its = st.its;
+    float3 &P = st.P, &acc = st.acc;
+    int &med = st.med, &depth = st.depth, &mode = st.mode, &ne = st.ne;
+    const float3 zero = mk(0.f, 0.f, 0.f);
     const AdjCtx *hook = pass_b ? &adj : nullptr;
-    bool alive = ray_intersect_ad<N>(sc, stack, ray, false, its, c);
-    for (int level = 0; alive && mode != 0; ++level) {
-        alive = false;
-        const float r1a = rng.next1(), r1b = rng.next1();
-        float r2[4];
-        r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
-        const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
-        DV<N> thr(mk(1.f, 1.f, 1.f));
-        const float3 dir_in = ray.d.val();
-        if (pass_b) adj.w = dot(gpix, total - acc) * rp.inv_spp;  // suffix radiance of this factor
-        if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c, hook)) {
-            // ------------------------------------------------ volumetric vertex
-            if (depth == 0 || thr.is_zero()) break;
-            const DevPhase &ph = sc.phases[sc.media[med].phase_id];
-            const float3 Q = cmul(P, thr.val());
-            DV<N> wo;
-            float pdf_nee;
-            if (mode & MODE_VOLUME_MAIN) {
-                const int k = ne++;
-                if (pass_b && k < kReplayEvents) {
-                    const float3 e = ev[k];
-                    adj.w = dot(gpix, e) * rp.inv_spp;
-                    nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c,
-                                    is_zero3(e, 0.f) ? nullptr : hook);
-                    acc = acc + e;
-                } else {
-                    const Rng saved = rng;
-                    DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
-                    float3 e = zero;
-                    if (!v.is_zero()) {
-                        const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
-                        if (pv.v > kEps)
-                            e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
-                    }
-                    if (pass_b && !is_zero3(e, 0.f)) {
-                        const Rng after = rng;
-                        rng = saved;
-                        adj.w = dot(gpix, e) * rp.inv_spp;
-                        DV<N> wo2;
-                        float pdf2;
-                        nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
-                        rng = after;
-                    }
-                    if (!pass_b && k < kReplayEvents) ev[k] = e;
-                    acc = acc + e;
-                }
-            }
-            const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
-            if (pvs.v > kEps) {
-                const float3 thr1 = thr.val() * pvs.v;
-                ray.d = wo;
-                ItsAD<N> its1;
-                const int k = ne++;
-                if (pass_b && k < kReplayEvents) {
-                    const float3 e = ev[k];
-                    adj.w = dot(gpix, e) * rp.inv_spp;
-                    look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr, nullptr,
-                                           c, is_zero3(e, 0.f) ? nullptr : hook);
-                    acc = acc + e;
-                } else {
-                    const Rng saved = rng;
-                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee,
-                                                       nullptr, nullptr, c);
-                    float3 e = zero;
-                    if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
-                        e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
-                    if (pass_b && !is_zero3(e, 0.f)) {
-                        const Rng after = rng;
-                        rng = saved;
-                        adj.w = dot(gpix, e) * rp.inv_spp;
-                        ItsAD<N> its2;
-                        float pdf2;
-                        look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr,
-                                               c, hook);
-                        rng = after;
-                    }
-                    if (!pass_b && k < kReplayEvents) ev[k] = e;
-                    acc = acc + e;
-                }
-                its = its1;
-                P = cmul(P, thr1);
-                depth -= 1;
-                mode &= ~MODE_EMISSION;
-                alive = true;
-            }
-            continue;
-        }
-        // ---------------------------------------------------- interface vertex
-        if (!its.valid() || thr.is_zero()) break;
-        const DevShape &sh = sc.shapes[its.shape];
-        if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) break;
+    bool alive = false;
+    const float r1a = rng.next1(), r1b = rng.next1();
+    float r2[4];
+    r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
+    const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
+    DV<N> thr(mk(1.f, 1.f, 1.f));
+    const float3 dir_in = ray.d.val();
+    if (pass_b) adj.w = dot(gpix, total - acc) * rp.inv_spp;  // suffix radiance of this factor
+    if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c, hook)) {
+        // ------------------------------------------------ volumetric vertex
+        if (depth == 0 || thr.is_zero()) return false;
+        const DevPhase &ph = sc.phases[sc.media[med].phase_id];
         const float3 Q = cmul(P, thr.val());
-        if (sh.light_id >= 0 && (mode & MODE_EMISSION)) acc = acc + cmul(Q, le_ad<N>(sc, its, -ray.d).val());
-        if (depth == 0) break;
-        const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
-        const bool is_null = b.type == BSDF_NULL;
-        const FrameAD<N> fr = its.frame();
-        const Its its0 = its.plain();
         DV<N> wo;
         float pdf_nee;
-        if (!is_null && (mode & MODE_SURFACE_MAIN)) {
+        if (mode & MODE_VOLUME_MAIN) {
             const int k = ne++;
             if (pass_b && k < kReplayEvents) {
                 const float3 e = ev[k];
                 adj.w = dot(gpix, e) * rp.inv_spp;
-                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c,
-                                  is_zero3(e, 0.f) ? nullptr : hook);
+                nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c,
+                                is_zero3(e, 0.f) ? nullptr : hook);
                 acc = acc + e;
             } else {
                 const Rng saved = rng;
-                DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+                DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
                 float3 e = zero;
                 if (!v.is_zero()) {
-                    const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
-                    const float bp = bsdf_pdf(b, its0.wi, wo.val());
-                    e = cmul(cmul(Q, v.val()), bv.val()) * mis_weight(pdf_nee, bp);
+                    const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+                    if (pv.v > kEps)
+                        e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
                 }
                 if (pass_b && !is_zero3(e, 0.f)) {
                     const Rng after = rng;
@@ -179,64 +119,158 @@ DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, 
                     adj.w = dot(gpix, e) * rp.inv_spp;
                     DV<N> wo2;
                     float pdf2;
-                    nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                    nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
                     rng = after;
                 }
                 if (!pass_b && k < kReplayEvents) ev[k] = e;
                 acc = acc + e;
             }
         }
-        float bpdf, beta;
-        const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
-        if (!bw.is_zero()) {
-            wo = fr.to_world(wo);
-            if (!is_null) wo = zero_grad(wo);
-            ray.o = its.p;
+        const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
+        if (pvs.v > kEps) {
+            const float3 thr1 = thr.val() * pvs.v;
             ray.d = wo;
-            const int med1 = is_transition(sh) ? target_medium(sc, its.shape, its.ng, wo.val()) : med;
-            float3 thr1 = thr.val();
             ItsAD<N> its1;
-            if (is_null) {
-                ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
+            const int k = ne++;
+            if (pass_b && k < kReplayEvents) {
+                const float3 e = ev[k];
+                adj.w = dot(gpix, e) * rp.inv_spp;
+                look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr, nullptr,
+                                       c, is_zero3(e, 0.f) ? nullptr : hook);
+                acc = acc + e;
             } else {
-                thr1 = cmul(thr1, bw.val());
-                const int k = ne++;
-                if (pass_b && k < kReplayEvents) {
-                    const float3 e = ev[k];
+                const Rng saved = rng;
+                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee,
+                                                   nullptr, nullptr, c);
+                float3 e = zero;
+                if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+                if (pass_b && !is_zero3(e, 0.f)) {
+                    const Rng after = rng;
+                    rng = saved;
                     adj.w = dot(gpix, e) * rp.inv_spp;
-                    look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee, nullptr, nullptr,
-                                           c, is_zero3(e, 0.f) ? nullptr : hook);
-                    acc = acc + e;
-                } else {
-                    const Rng saved = rng;
-                    DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee,
-                                                       nullptr, nullptr, c);
-                    float3 e = zero;
-                    if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
-                        e = cmul(cmul(P, thr1), att.val()) * mis_weight(bpdf, pdf_nee);
-                    if (pass_b && !is_zero3(e, 0.f)) {
-                        const Rng after = rng;
-                        rng = saved;
-                        adj.w = dot(gpix, e) * rp.inv_spp;
-                        ItsAD<N> its2;
-                        float pdf2;
-                        look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its2, pdf2, nullptr,
-                                               nullptr, c, hook);
-                        rng = after;
-                    }
-                    if (!pass_b && k < kReplayEvents) ev[k] = e;
-                    acc = acc + e;
+                    ItsAD<N> its2;
+                    float pdf2;
+                    look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr,
+                                           c, hook);
+                    rng = after;
                 }
-                mode &= ~MODE_EMISSION;
+                if (!pass_b && k < kReplayEvents) ev[k] = e;
+                acc = acc + e;
             }
             its = its1;
             P = cmul(P, thr1);
-            med = med1;
             depth -= 1;
+            mode &= ~MODE_EMISSION;
             alive = true;
         }
+        return alive;
     }
-    return acc;
+    // ---------------------------------------------------- interface vertex
+    if (!its.valid() || thr.is_zero()) return false;
+    const DevShape &sh = sc.shapes[its.shape];
+    if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) return false;
+    const float3 Q = cmul(P, thr.val());
+    if (sh.light_id >= 0 && (mode & MODE_EMISSION)) acc = acc + cmul(Q, le_ad<N>(sc, its, -ray.d).val());
+    if (depth == 0) return false;
+    const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
+    const bool is_null = b.type == BSDF_NULL;
+    const FrameAD<N> fr = its.frame();
+    const Its its0 = its.plain();
+    DV<N> wo;
+    float pdf_nee;
+    if (!is_null && (mode & MODE_SURFACE_MAIN)) {
+        const int k = ne++;
+        if (pass_b && k < kReplayEvents) {
+            const float3 e = ev[k];
+            adj.w = dot(gpix, e) * rp.inv_spp;
+            nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c,
+                              is_zero3(e, 0.f) ? nullptr : hook);
+            acc = acc + e;
+        } else {
+            const Rng saved = rng;
+            DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+            float3 e = zero;
+            if (!v.is_zero()) {
+                const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
+                const float bp = bsdf_pdf(b, its0.wi, wo.val());
+                e = cmul(cmul(Q, v.val()), bv.val()) * mis_weight(pdf_nee, bp);
+            }
+            if (pass_b && !is_zero3(e, 0.f)) {
+                const Rng after = rng;
+                rng = saved;
+                adj.w = dot(gpix, e) * rp.inv_spp;
+                DV<N> wo2;
+                float pdf2;
+                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                rng = after;
+            }
+            if (!pass_b && k < kReplayEvents) ev[k] = e;
+            acc = acc + e;
+        }
+    }
+    float bpdf, beta;
+    const DV<N> bw = bsdf_sample_ad<N>(b, its, fr, its0, r3a, r3b, r3c, wo, bpdf, beta);
+    if (!bw.is_zero()) {
+        wo = fr.to_world(wo);
+        if (!is_null) wo = zero_grad(wo);
+        ray.o = its.p;
+        ray.d = wo;
+        const int med1 = is_transition(sh) ? target_medium(sc, its.shape, its.ng, wo.val()) : med;
+        float3 thr1 = thr.val();
+        ItsAD<N> its1;
+        if (is_null) {
+            ray_intersect_ad<N>(sc, stack, ray, true, its1, c);
+        } else {
+            thr1 = cmul(thr1, bw.val());
+            const int k = ne++;
+            if (pass_b && k < kReplayEvents) {
+                const float3 e = ev[k];
+                adj.w = dot(gpix, e) * rp.inv_spp;
+                look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee, nullptr, nullptr,
+                                       c, is_zero3(e, 0.f) ? nullptr : hook);
+                acc = acc + e;
+            } else {
+                const Rng saved = rng;
+                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its1, pdf_nee,
+                                                   nullptr, nullptr, c);
+                float3 e = zero;
+                if (!att.is_zero() && (mode & MODE_SURFACE_MAIN))
+                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(bpdf, pdf_nee);
+                if (pass_b && !is_zero3(e, 0.f)) {
+                    const Rng after = rng;
+                    rng = saved;
+                    adj.w = dot(gpix, e) * rp.inv_spp;
+                    ItsAD<N> its2;
+                    float pdf2;
+                    look_for_emitter_ad<N>(sc, stack, ray, true, rng, med1, depth - 1, its2, pdf2, nullptr,
+                                           nullptr, c, hook);
+                    rng = after;
+                }
+                if (!pass_b && k < kReplayEvents) ev[k] = e;
+                acc = acc + e;
+            }
+            mode &= ~MODE_EMISSION;
+        }
+        its = its1;
+        P = cmul(P, thr1);
+        med = med1;
+        depth -= 1;
+        alive = true;
+    }
+    return alive;
+}
+
+template <int N>
+DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, long long g, bool pass_b, float3 total,
+                        float3 gpix, AdjCtx &adj, Ctr &c, float3 *ev) {
+    AdjState<N> st;
+    bool alive = replay_start<N>(sc, rp, stack, g, st, c);
+    while (alive && st.mode != 0) {
+        alive = replay_step<N>(sc, rp, stack, pass_b, total, gpix, adj, c, ev, st);
+        ++st.level;
+    }
+    return st.acc;
 }
 
 // One camera path (index gi of the launch's range): pass A (value), then pass B (scatter)
@@ -253,11 +287,11 @@ DT_D void adjoint_one(const DevScene &sc, const RenderParams &rp, int *stack, lo
     float3 ev[kReplayEvents];
     float3 total = mk(0.f, 0.f, 0.f);
     if (active) {
-        total = replay_path<N>(sc, rp, stack, g, pixel, false, total, total, adj, c, ev);
+        total = replay_path<N>(sc, rp, stack, g, false, total, total, adj, c, ev);
         if (grad != nullptr && dimg != nullptr && !is_zero3(total, 0.f)) {
             const float3 gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1),
                                  __ldg(dimg + 3 * (size_t)pixel + 2));
-            if (!is_zero3(gp, 0.f)) replay_path<N>(sc, rp, stack, g, pixel, true, total, gp, adj, c, ev);
+            if (!is_zero3(gp, 0.f)) replay_path<N>(sc, rp, stack, g, true, total, gp, adj, c, ev);
         }
     }
     if (img_acc != nullptr) {
@@ -283,6 +317,92 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp
     adjoint_one<N>(sc, rp, s_stack + threadIdx.x, (long long)blockIdx.x * kBlock + threadIdx.x, dimg, grad, img_acc, c,
                    stride);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// Wavefront schedule of the replay: pass A and pass B each run one launch per path
+// vertex over the paths still alive (compacted path-index queues, as k_cam_level).
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams rp, AdjState<N> *states, int *q_out,
+                                                      unsigned long long *cnt_out, const float *dimg,
+                                                      const float3 *totals, bool pass_b, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    bool live = false;
+    if (gi < rp.path_count) {
+        const long long g = rp.path_begin + gi;
+        bool run = true;
+        if (pass_b) {  // pass B only for paths with a value whose pixel has a non-zero dL/dI
+            const int pixel = (int)(g / rp.spp);
+            const float3 gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1),
+                                 __ldg(dimg + 3 * (size_t)pixel + 2));
+            run = !is_zero3(totals[gi], 0.f) && !is_zero3(gp, 0.f);
+        }
+        if (run) {
+            AdjState<N> st;
+            live = replay_start<N>(sc, rp, stack, g, st, c) && st.mode != 0;
+            states[gi] = st;
+        }
+    }
+    push_path(q_out, cnt_out, (int)gi, live);
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_adj_level(DevScene sc, RenderParams rp, AdjState<N> *states, const int *q_in,
+                                                      const unsigned long long *cnt_in, int *q_out,
+                                                      unsigned long long *cnt_out, const float *dimg, float *grad,
+                                                      const float3 *totals, float3 *evbuf, bool pass_b,
+                                                      unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long n = (long long)*cnt_in;
+    Ctr c;
+    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
+        const int id = q_in[i];
+        AdjState<N> st = states[id];
+        const float3 zero = mk(0.f, 0.f, 0.f);
+        float3 total = zero, gp = zero;
+        if (pass_b) {
+            const int pixel = (int)((rp.path_begin + id) / rp.spp);
+            total = totals[id];
+            gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1), __ldg(dimg + 3 * (size_t)pixel + 2));
+        }
+        AdjCtx adj{grad, 0.f};
+        const bool alive = replay_step<N>(sc, rp, stack, pass_b, total, gp, adj, c, evbuf + (size_t)id * kReplayEvents, st);
+        ++st.level;
+        states[id] = st;
+        push_path(q_out, cnt_out, id, alive && st.mode != 0);
+    }
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// after pass A: each path's value (pass B's suffix base) and the image sum in path order
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_adj_totals(RenderParams rp, const AdjState<N> *states, float3 *totals,
+                                                       double *img_acc) {
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < rp.path_count;
+    const long long g = rp.path_begin + (active ? gi : 0);
+    const int pixel = (int)(g / rp.spp);
+    float3 total = mk(0.f, 0.f, 0.f);
+    if (active) {
+        total = states[gi].acc;
+        totals[gi] = total;
+    }
+    if (img_acc != nullptr) {
+        const unsigned full = 0xffffffffu;
+        const int p0 = __shfl_sync(full, pixel, 0);
+        const bool uniform = __all_sync(full, active && pixel == p0);
+        float v[3] = {total.x * rp.inv_spp, total.y * rp.inv_spp, total.z * rp.inv_spp};
+        if (uniform)
+            for (int k = 0; k < 3; ++k)
+                for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(full, v[k], off);
+        if (active && (!uniform || (threadIdx.x & 31) == 0))
+            for (int k = 0; k < 3; ++k)
+                if (v[k] != 0.f) atomicAdd(img_acc + (size_t)pixel * 3 + k, (double)v[k]);
+    }
 }
 
 // Image write rule of integratorAD.cpp:59-87 (a pixel is written only if non-negative).

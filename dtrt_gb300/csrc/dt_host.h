@@ -28,6 +28,9 @@ struct Scratch {
     // wavefront camera schedule: per-path state, two path-index queues, per-level counts
     void *cam_state = nullptr, *cam_q = nullptr, *cam_cnt = nullptr;
     size_t cam_state_bytes = 0, cam_q_bytes = 0, cam_cnt_bytes = 0;
+    // wavefront density replay: per-path values of pass A and its event values
+    void *adj_tot = nullptr, *adj_ev = nullptr;
+    size_t adj_tot_bytes = 0, adj_ev_bytes = 0;
 };
 
 // Connectivity kept from the last build, so that a rebuild from a description with the

@@ -395,6 +395,9 @@ __global__ void __launch_bounds__(kBlock) k_camera(DevScene sc, RenderParams rp,
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
+// AUTO schedule: the wavefront from this many camera paths per render batch
+constexpr long long kWavefrontMinPaths = 1 << 16;
+
 // Wavefront schedule: paths that continue are compacted into a queue of path indices
 // after every vertex, so each launch runs one vertex of live paths only (a warp no longer
 // idles on the paths of its lanes that ended early).

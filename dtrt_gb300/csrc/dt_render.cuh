@@ -27,9 +27,6 @@ namespace dt {
         }                                                                            \
     } while (0)
 
-// AUTO camera schedule: the wavefront from this many paths per batch
-constexpr long long kWavefrontMinPaths = 1 << 16;
-
 template <int N>
 int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t st) {
     using clk = std::chrono::steady_clock;
@@ -109,6 +106,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     };
     auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
     uint64_t tot_edge = 0, tot_lins = 0, tot_li = 0, batches = 0;
+    bool used_wavefront = false;
     int rc = DTRT_OK;
     // Li tasks are drained chunk by chunk so that the queue never exceeds li_cap
     auto drain_li = [&]() -> int {
@@ -143,6 +141,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         }
         int sms = 0;
         DT_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+        used_wavefront = wavefront;
         CamState<N> *states = (CamState<N> *)sb.cam_state;
         int *qa = (int *)sb.cam_q, *qb = qa + Bw;
         unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt;
@@ -228,6 +227,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     ls.batches = batches;
     ls.kernel_launches = launches;
     ls.counters_enabled = ctr != nullptr;
+    ls.camera_schedule = used_wavefront ? DTRT_CAMERA_WAVEFRONT : DTRT_CAMERA_MEGAKERNEL;
     for (int k = 0; k < 5; ++k) {
         ls.k_rays[k] = hc[4 * k];
         ls.k_node_visits[k] = hc[4 * k + 1];

@@ -190,6 +190,7 @@ typedef struct {
     double ms_primary;        /* primary-edge kernel(s)                             */
     double ms_setup;          /* scene upload / derived data for this render        */
     int counters_enabled;
+    int camera_schedule;      /* DTRT_CAMERA_MEGAKERNEL or DTRT_CAMERA_WAVEFRONT (forward renders) */
 } dtrt_render_stats;
 
 /* Opaque scene handle (device-resident geometry, BVH, media, edge tables). */

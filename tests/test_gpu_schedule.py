@@ -47,3 +47,21 @@ def test_schedule_argument_checks():
         ns.set_camera_schedule("auto")
         img = ns.render(seed=1, spp=4, max_bounces=3, sppe=0, sppse=0)
         assert np.isfinite(img).all()
+
+
+def test_density_adjoint_wavefront_equals_megakernel():
+    """The density replay under both schedules: the same image (pass A sums in path
+    order) and the same gradient up to the order of its FP32 atomic sums."""
+    spec = scenes.config3(40, 40, res=16, nder=1, param_slots=False, nblobs=6)
+    dimg = np.random.default_rng(4).normal(size=(40, 40, 3)).astype(np.float32)
+    kw = dict(seed=13, spp=16, max_bounces=8, sppe=0, sppse=0)
+    out = {}
+    with native.NativeScene(spec) as ns:
+        for sched in ("megakernel", "wavefront"):
+            ns.set_camera_schedule(sched)
+            out[sched] = ns.render_adjoint(dimg, **kw)
+            assert ns.last_stats()["camera_schedule"] == {"megakernel": 1, "wavefront": 2}[sched]
+    (ia, ga), (ib, gb) = out["megakernel"], out["wavefront"]
+    assert np.array_equal(ia, ib) and ia.sum() > 0
+    assert np.abs(ga).max() > 0
+    assert np.abs(ga - gb).max() <= 1e-4 * np.abs(ga).max()

@@ -32,6 +32,60 @@ cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const flo
     return cudaGetLastError();
 }
 
+size_t AdjWave::bytes(long long cap, int levels) {
+    return (size_t)cap * (sizeof(AdjState<1>) + 2 * sizeof(int) + sizeof(float3) + kReplayEvents * sizeof(float3)) +
+           (size_t)2 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 5 arrays
+}
+
+void AdjWave::carve(void *base, long long capacity, int lv) {
+    char *p = (char *)base;
+    auto take = [&](size_t n) {
+        void *r = p;
+        p += (n + 255) & ~(size_t)255;
+        return r;
+    };
+    cap = capacity;
+    levels = lv;
+    states = take((size_t)cap * sizeof(AdjState<1>));
+    q = (int *)take((size_t)2 * cap * sizeof(int));
+    tots = (float3 *)take((size_t)cap * sizeof(float3));
+    ev = (float3 *)take((size_t)cap * kReplayEvents * sizeof(float3));
+    cnt = (unsigned long long *)take((size_t)2 * (levels + 1) * sizeof(unsigned long long));
+}
+
+// Wavefront replay of paths [rp.path_begin, +rp.path_count) in chunks of the workspace's
+// capacity: pass A (values, image) then, with a gradient, pass B (scatter); each pass is
+// a start launch, one launch per vertex level over the live paths, (A) a totals launch.
+cudaError_t launch_adjoint_wave(const DevScene &sc, const RenderParams &range, const float *dimg, float *grad,
+                                double *img_acc, unsigned long long *ctr, const AdjWave &w, int sms, cudaStream_t st,
+                                uint64_t *launches) {
+    const int levels = range.max_bounces + 1;
+    if (levels > w.levels) return cudaErrorInvalidValue;
+    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
+    AdjState<1> *states = (AdjState<1> *)w.states;
+    int *qa = w.q, *qb = w.q + w.cap;
+    const bool pass_b = grad != nullptr && dimg != nullptr;
+    RenderParams rp = range;
+    for (long long b0 = 0; b0 < range.path_count; b0 += w.cap) {
+        rp.path_begin = range.path_begin + b0;
+        rp.path_count = std::min(w.cap, range.path_count - b0);
+        const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
+        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)2 * (levels + 1) * sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return e;
+        for (int pass = 0; pass < (pass_b ? 2 : 1); ++pass) {
+            unsigned long long *cnt = w.cnt + pass * (levels + 1);
+            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, cnt, dimg, w.tots, pass == 1, ctr);
+            for (int L = 0; L < levels; ++L)
+                k_adj_level<1><<<gw, kBlock, 0, st>>>(sc, rp, states, (L & 1) ? qb : qa, cnt + L, (L & 1) ? qa : qb,
+                                                     cnt + L + 1, dimg, grad, w.tots, w.ev, pass == 1, ctr);
+            if (pass == 0) k_adj_totals<1><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, w.tots, img_acc);
+            if (launches) *launches += levels + 1 + (pass == 0 ? 1 : 0);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
                    int on_device, cudaStream_t st) {
     using clk = std::chrono::steady_clock;
@@ -110,51 +164,33 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     DT_ACK(cudaEventRecord(e0, st));
     // schedule: the wavefront (pass A and pass B each one launch per vertex over the live
     // paths) for large renders, as dtrt_render_fwd's camera schedule
-    long long B = 1ll << 24;  // paths per launch (megakernel) or per wavefront chunk
+    const long long B = 1ll << 24;  // paths per megakernel launch
     bool wavefront = s->camera_schedule == DTRT_CAMERA_WAVEFRONT ||
                      (s->camera_schedule == DTRT_CAMERA_AUTO && total >= kWavefrontMinPaths);
-    const int levels = o->max_bounces + 1;
+    AdjWave w{};
     if (wavefront) {
-        B = std::min<long long>(1ll << 22, std::max<long long>(total, 1));
-        if (!(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, (size_t)B * sizeof(AdjState<1>)) &&
-              ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)2 * B * sizeof(int)) &&
-              ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)2 * (levels + 1) * sizeof(unsigned long long)) &&
-              ensure_buffer(&sb.adj_tot, &sb.adj_tot_bytes, (size_t)B * sizeof(float3)) &&
-              ensure_buffer(&sb.adj_ev, &sb.adj_ev_bytes, (size_t)B * kReplayEvents * sizeof(float3)))) {
+        const long long cap = std::min<long long>(1ll << 22, std::max<long long>(total, 1));
+        if (ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, AdjWave::bytes(cap, o->max_bounces + 1))) {
+            w.carve(sb.cam_state, cap, o->max_bounces + 1);
+        } else {
             if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
             cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
             wavefront = false;
-            B = 1ll << 24;
         }
     }
-    int sms = 0;
-    DT_ACK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
-    AdjState<1> *states = (AdjState<1> *)sb.cam_state;
-    int *qa = (int *)sb.cam_q, *qb = qa + B;
-    unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt;
-    float3 *tots = (float3 *)sb.adj_tot, *evb = (float3 *)sb.adj_ev;
-    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
-    for (long long b0 = 0; b0 < total; b0 += B) {
-        rp.path_begin = b0;
-        rp.path_count = std::min(B, total - b0);
-        if (!wavefront) {
+    if (wavefront) {
+        int sms = 0;
+        DT_ACK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+        rp.path_begin = 0;
+        rp.path_count = total;
+        DT_ACK(launch_adjoint_wave(sc, rp, dimg, grad, img_acc, ctr, w, sms, st, &launches));
+    } else {
+        for (long long b0 = 0; b0 < total; b0 += B) {
+            rp.path_begin = b0;
+            rp.path_count = std::min(B, total - b0);
             DT_ACK(launch_adjoint(sc, rp, dimg, grad, img_acc, ctr, 1, st));
             ++launches;
-            continue;
         }
-        const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
-        const bool pass_b = grad != nullptr && dimg != nullptr;
-        DT_ACK(cudaMemsetAsync(lcnt, 0, (size_t)2 * (levels + 1) * sizeof(unsigned long long), st));
-        for (int pass = 0; pass < (pass_b ? 2 : 1); ++pass) {
-            unsigned long long *cnt = lcnt + pass * (levels + 1);
-            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, cnt, dimg, tots, pass == 1, ctr);
-            for (int L = 0; L < levels; ++L)
-                k_adj_level<1><<<gw, kBlock, 0, st>>>(sc, rp, states, (L & 1) ? qb : qa, cnt + L, (L & 1) ? qa : qb,
-                                                     cnt + L + 1, dimg, grad, tots, evb, pass == 1, ctr);
-            if (pass == 0) k_adj_totals<1><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, tots, img_acc);
-            launches += levels + 1 + (pass == 0 ? 1 : 0);
-        }
-        DT_ACK(cudaGetLastError());
     }
     DT_ACK(cudaEventRecord(e1, st));
     if (image) {
@@ -181,7 +217,7 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     std::memset(&ls, 0, sizeof(ls));
     ls.camera_paths = (uint64_t)total;
     ls.kernel_launches = launches;
-    ls.batches = (uint64_t)((total + B - 1) / B);
+    ls.batches = (uint64_t)((total + (wavefront ? w.cap : B) - 1) / std::max<long long>(1, wavefront ? w.cap : B));
     ls.counters_enabled = ctr != nullptr;
     ls.camera_schedule = wavefront ? DTRT_CAMERA_WAVEFRONT : DTRT_CAMERA_MEGAKERNEL;
     ls.k_rays[0] = ls.rays = hc[0];

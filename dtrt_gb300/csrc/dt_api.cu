@@ -1000,8 +1000,7 @@ void free_scene(dtrt_scene *s) {
     s->dgrid_bufs.clear();
     Scratch &b = s->scratch;
     void *ptrs[] = {b.acc1,     b.acc2,     b.out,     b.qe,     b.ql,      b.qli,       b.counts,   b.err,
-                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt,
-                    b.adj_tot,  b.adj_ev};
+                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     b = Scratch();

@@ -135,6 +135,10 @@ struct dtrt_batch {
     std::vector<cudaStream_t> side;  // streams 1.. of the per-item schedule
     std::vector<cudaEvent_t> side_ev;
     cudaEvent_t fork_ev = nullptr;
+    // wavefront replay workspaces of the per-item schedule, one per stream (empty: megakernel)
+    std::vector<void *> wave_mem;
+    std::vector<dt::AdjWave> wave;
+    int sms = 0;
     // graph
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -161,6 +165,7 @@ void free_batch(dtrt_batch *b) {
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    for (void *p : b->wave_mem) cudaFree(p);
     void *ptrs[] = {b->d_items, b->d_cbeg, b->d_order, b->d_imgs, b->d_next, b->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -222,6 +227,11 @@ int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long 
         }
         if (stride > 1) {
             DT_BCK(launch_adjoint(it.sc, it.rp, it.dimg, it.grad, it.img_acc, nullptr, stride, q));
+            continue;
+        }
+        if (!b->wave.empty()) {  // the wavefront replay of dtrt_render_adjoint, on this stream's workspace
+            DT_BCK(launch_adjoint_wave(it.sc, it.rp, it.dimg, it.grad, it.img_acc, nullptr, b->wave[i % S], b->sms, q,
+                                       nullptr));
             continue;
         }
         RenderParams rp = it.rp;  // launches of at most 2^24 paths, as dtrt_render_adjoint
@@ -540,6 +550,33 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
         b->side.push_back(x);
         DT_BCK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         b->side_ev.push_back(ev);
+    }
+    // wavefront workspaces for the per-item schedule (4 streams), as dtrt_render_adjoint's
+    {
+        long long maxp = 0;
+        int maxl = 1;
+        for (int i = 0; i < n; ++i) {
+            maxp = std::max(maxp, b->paths[i]);
+            maxl = std::max(maxl, items[i].opts.max_bounces + 1);
+        }
+        b->sms = sms;
+        if (maxp >= kWavefrontMinPaths) {
+            const long long cap = std::min<long long>(1ll << 22, maxp);
+            for (int k = 0; k < 4; ++k) {
+                void *p = nullptr;
+                if (cudaMalloc(&p, AdjWave::bytes(cap, maxl)) != cudaSuccess) {
+                    cudaGetLastError();  // no room: the per-item schedule runs the megakernel
+                    for (void *x : b->wave_mem) cudaFree(x);
+                    b->wave_mem.clear();
+                    b->wave.clear();
+                    break;
+                }
+                b->wave_mem.push_back(p);
+                AdjWave w;
+                w.carve(p, cap, maxl);
+                b->wave.push_back(w);
+            }
+        }
     }
     b->order.resize(n);
     std::iota(b->order.begin(), b->order.end(), 0);

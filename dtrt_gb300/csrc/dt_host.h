@@ -28,9 +28,7 @@ struct Scratch {
     // wavefront camera schedule: per-path state, two path-index queues, per-level counts
     void *cam_state = nullptr, *cam_q = nullptr, *cam_cnt = nullptr;
     size_t cam_state_bytes = 0, cam_q_bytes = 0, cam_cnt_bytes = 0;
-    // wavefront density replay: per-path values of pass A and its event values
-    void *adj_tot = nullptr, *adj_ev = nullptr;
-    size_t adj_tot_bytes = 0, adj_ev_bytes = 0;
+
 };
 
 // Connectivity kept from the last build, so that a rebuild from a description with the
@@ -77,6 +75,21 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
                    int on_device, cudaStream_t stream);
 cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const float *dimg, float *grad, double *img_acc,
                            unsigned long long *ctr, long long stride, cudaStream_t st);
+// Device workspace of the wavefront density replay: path states, two path-index queues,
+// pass-A values and event values for `cap` paths, level counts of both passes.
+struct AdjWave {
+    void *states = nullptr;
+    int *q = nullptr;
+    float3 *tots = nullptr, *ev = nullptr;
+    unsigned long long *cnt = nullptr;
+    long long cap = 0;
+    int levels = 0;
+    static size_t bytes(long long cap, int levels);
+    void carve(void *base, long long cap, int levels);  // lay the arrays out in one allocation
+};
+cudaError_t launch_adjoint_wave(const DevScene &sc, const RenderParams &range, const float *dimg, float *grad,
+                                double *img_acc, unsigned long long *ctr, const AdjWave &w, int sms, cudaStream_t st,
+                                uint64_t *launches);
 int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image,
                           float *d_vertices, int on_device, cudaStream_t stream);
 template <int N>

@@ -175,12 +175,36 @@ DT_D bool camera_start(const DevScene &sc, const RenderParams &rp, int *stack, l
     return ray_intersect_ad<N>(sc, stack, st.ray, false, st.its, c);
 }
 
-// One vertex of camera path g: a volume vertex (NEE, volume edge record, phase sampling)
-// or an interface vertex (emission, Lins and surface edge records, NEE, BSDF sampling).
-// Returns whether the path continues; st.level is advanced by the caller.
+// Random numbers of a vertex drawn before its branch, the distance-sampling throughput and
+// the incoming direction: what the volume and interface halves of a vertex share.
 template <int N>
-DT_D bool camera_step(const DevScene &sc, const RenderParams &rp, int *stack, long long g, CamState<N> &st,
-                      const Queue &qe, const Queue &ql, Ctr &c) {
+struct VertexIn {
+    float r2[4], r3a, r3b, r3c;
+    DV<N> thr;
+    float3 dir_in;
+};
+
+// First part of a vertex of camera path g (volpathAD.cpp:160-164, 306-308): the vertex's
+// random numbers and distance sampling. 0: the path ends here, 1: volume vertex, 2:
+// interface vertex.
+template <int N>
+DT_D int camera_decide(const DevScene &sc, CamState<N> &st, VertexIn<N> &vin, Ctr &c) {
+    Rng &rng = st.rng;
+    const float r1a = rng.next1(), r1b = rng.next1();
+    vin.r2[0] = rng.next1(); vin.r2[1] = rng.next1(); vin.r2[2] = rng.next1(); vin.r2[3] = rng.next1();
+    vin.r3a = rng.next1(); vin.r3b = rng.next1(); vin.r3c = rng.next1();
+    vin.thr = DV<N>(mk(1.f, 1.f, 1.f));
+    vin.dir_in = st.ray.d.val();
+    if (st.med >= 0 && sample_distance_ad<N>(sc, sc.media[st.med], st.ray, st.its.t, r1a, r1b, rng, vin.thr, c))
+        return (st.depth == 0 || vin.thr.is_zero()) ? 0 : 1;
+    return (!st.its.valid() || vin.thr.is_zero()) ? 0 : 2;
+}
+
+// Volume vertex (volpathAD.cpp:164-305): NEE, volume edge record, phase sampling and the
+// emitter lookup along the new direction. Returns whether the path continues.
+template <int N>
+DT_D bool camera_volume(const DevScene &sc, const RenderParams &rp, int *stack, long long g, CamState<N> &st,
+                        const VertexIn<N> &vin, const Queue &qe, Ctr &c) {
     Rng &rng = st.rng;
     RayAD<N> &ray = st.ray;
     ItsAD<N> &its = st.its;
@@ -189,65 +213,80 @@ DT_D bool camera_step(const DevScene &sc, const RenderParams &rp, int *stack, lo
     const int level = st.level;
     const int pixel = (int)(g / rp.spp);
     const uint64_t key = (uint64_t)g;
+    const float *r2 = vin.r2;
+    const float r3a = vin.r3a, r3b = vin.r3b;
+    const DV<N> &thr = vin.thr;
+    const float3 dir_in = vin.dir_in;
     bool alive = false;
-    const float r1a = rng.next1(), r1b = rng.next1();
-    float r2[4];
-    r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
-    const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
-    DV<N> thr(mk(1.f, 1.f, 1.f));
-    const float3 dir_in = ray.d.val();
-    if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c)) {
-        // ------------------------------------------------ volumetric vertex, volpathAD.cpp:164-305
-        if (depth == 0 || thr.is_zero()) return false;
-        const DevPhase &ph = sc.phases[sc.media[med].phase_id];
-        const DV<N> Q = cmul(P, thr);
-        DV<N> wo;
-        float pdf_nee;
-        if (mode & MODE_VOLUME_MAIN) {
-            DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
-            if (!v.is_zero()) {
-                Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
-                if (pv.v > kEps) acc += cmul(Q, v) * (pv * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
-            }
+    // ------------------------------------------------ volumetric vertex, volpathAD.cpp:164-305
+    const DevPhase &ph = sc.phases[sc.media[med].phase_id];
+    const DV<N> Q = cmul(P, thr);
+    DV<N> wo;
+    float pdf_nee;
+    if (mode & MODE_VOLUME_MAIN) {
+        DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
+        if (!v.is_zero()) {
+            Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+            if (pv.v > kEps) acc += cmul(Q, v) * (pv * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
         }
-        // edge record before the continuation overwrites the vertex state
-        if (rp.sppse > 0 && (mode & MODE_VOLUME_BOUNDARY2) && sc.has_edges &&
-            (sc.moving_geometry || !ray.o.der_zero(0.f))) {
-            const long long slot = queue_reserve(sc, qe);
-            if (slot >= 0) {
-                EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
-                const float3 x = ray.o.val(), w = cmul(P.val(), thr.val()) * rp.inv_spp, wi = -dir_in;
-                r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
-#pragma unroll
-                for (int j = 0; j < N; ++j) {
-                    const float3 gj = ray.o.grad(j);
-                    r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
-                }
-                r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
-                r.wi[0] = wi.x; r.wi[1] = wi.y; r.wi[2] = wi.z;
-                r.kind = 1; r.shape = -1; r.med = med; r.phase = sc.media[med].phase_id;
-                r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 1u, (uint32_t)level);
-            }
-        }
-        const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
-        if (pvs.v > kEps) {
-            const DV<N> thr1 = thr * pvs;
-            ray.d = wo;
-            ItsAD<N> its1;
-            DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
-                                               nullptr, c);
-            if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
-                acc += cmul(cmul(P, thr1), att) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
-            its = its1;
-            P = cmul(P, thr1);
-            depth -= 1;
-            mode &= ~MODE_EMISSION;
-            alive = true;
-        }
-        return alive;
     }
+    // edge record before the continuation overwrites the vertex state
+    if (rp.sppse > 0 && (mode & MODE_VOLUME_BOUNDARY2) && sc.has_edges &&
+        (sc.moving_geometry || !ray.o.der_zero(0.f))) {
+        const long long slot = queue_reserve(sc, qe);
+        if (slot >= 0) {
+            EdgeRec<N> &r = reinterpret_cast<EdgeRec<N> *>(qe.data)[slot];
+            const float3 x = ray.o.val(), w = cmul(P.val(), thr.val()) * rp.inv_spp, wi = -dir_in;
+            r.x0[0] = x.x; r.x0[1] = x.y; r.x0[2] = x.z;
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+                const float3 gj = ray.o.grad(j);
+                r.x0d[j][0] = gj.x; r.x0d[j][1] = gj.y; r.x0d[j][2] = gj.z;
+            }
+            r.w[0] = w.x; r.w[1] = w.y; r.w[2] = w.z;
+            r.wi[0] = wi.x; r.wi[1] = wi.y; r.wi[2] = wi.z;
+            r.kind = 1; r.shape = -1; r.med = med; r.phase = sc.media[med].phase_id;
+            r.depth = depth - 1; r.pixel = pixel; r.key = child_key(key, 1u, (uint32_t)level);
+        }
+    }
+    const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
+    if (pvs.v > kEps) {
+        const DV<N> thr1 = thr * pvs;
+        ray.d = wo;
+        ItsAD<N> its1;
+        DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr,
+                                           nullptr, c);
+        if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+            acc += cmul(cmul(P, thr1), att) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+        its = its1;
+        P = cmul(P, thr1);
+        depth -= 1;
+        mode &= ~MODE_EMISSION;
+        alive = true;
+    }
+    return alive;
+}
+
+// Interface vertex (volpathAD.cpp:306-617): emission, Lins and surface edge records, NEE,
+// BSDF sampling and the emitter lookup (or null-interface crossing). Returns whether the
+// path continues.
+template <int N>
+DT_D bool camera_surface(const DevScene &sc, const RenderParams &rp, int *stack, long long g, CamState<N> &st,
+                         const VertexIn<N> &vin, const Queue &qe, const Queue &ql, Ctr &c) {
+    Rng &rng = st.rng;
+    RayAD<N> &ray = st.ray;
+    ItsAD<N> &its = st.its;
+    DV<N> &P = st.P, &acc = st.acc;
+    int &med = st.med, &depth = st.depth, &mode = st.mode;
+    const int level = st.level;
+    const int pixel = (int)(g / rp.spp);
+    const uint64_t key = (uint64_t)g;
+    const float *r2 = vin.r2;
+    const float r3a = vin.r3a, r3b = vin.r3b, r3c = vin.r3c;
+    const DV<N> &thr = vin.thr;
+    const float3 dir_in = vin.dir_in;
+    bool alive = false;
     // ---------------------------------------------------- interface vertex, volpathAD.cpp:306-617
-    if (!its.valid() || thr.is_zero()) return false;
     const DevShape &sh = sc.shapes[its.shape];
     if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) return false;
     const DV<N> Q = cmul(P, thr);
@@ -340,6 +379,18 @@ DT_D bool camera_step(const DevScene &sc, const RenderParams &rp, int *stack, lo
     return alive;
 }
 
+// One vertex of camera path g. Returns whether the path continues; st.level is advanced
+// by the caller.
+template <int N>
+DT_D bool camera_step(const DevScene &sc, const RenderParams &rp, int *stack, long long g, CamState<N> &st,
+                      const Queue &qe, const Queue &ql, Ctr &c) {
+    VertexIn<N> vin;
+    const int kind = camera_decide<N>(sc, st, vin, c);
+    if (kind == 1) return camera_volume<N>(sc, rp, stack, g, st, vin, qe, c);
+    if (kind == 2) return camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c);
+    return false;
+}
+
 // FP64 pixel accumulation of a path's contribution (already divided by spp): a warp
 // whose 32 lanes share one pixel reduces with shuffles first. Every lane of the warp calls it.
 template <int N>
@@ -429,11 +480,37 @@ __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams 
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
+// Vertex level L, first part: random numbers and distance sampling of every live path,
+// which is then queued as a volume or an interface vertex (or ends).
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_cam_level(DevScene sc, RenderParams rp, CamState<N> *states, const int *q_in,
-                                                      const unsigned long long *cnt_in, int *q_out,
-                                                      unsigned long long *cnt_out, Queue qe, Queue ql,
-                                                      unsigned long long *ctr) {
+__global__ void __launch_bounds__(kBlock) k_cam_decide(DevScene sc, RenderParams rp, CamState<N> *states,
+                                                       VertexIn<N> *vins, const int *q_in,
+                                                       const unsigned long long *cnt_in, int *qv,
+                                                       unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s,
+                                                       unsigned long long *ctr) {
+    const long long n = (long long)*cnt_in;
+    Ctr c;
+    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
+        const int id = q_in[i];
+        CamState<N> st = states[id];
+        VertexIn<N> vin;
+        const int kind = camera_decide<N>(sc, st, vin, c);
+        states[id] = st;
+        if (kind) vins[id] = vin;
+        push_path(qv, cnt_v, id, kind == 1);
+        push_path(qs, cnt_s, id, kind == 2);
+    }
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// Vertex level L, second part: the volume (kVolume) or interface vertices of the level;
+// continuing paths go to the queue of level L+1.
+template <int N, bool kVolume>
+__global__ void __launch_bounds__(kBlock) k_cam_vertex(DevScene sc, RenderParams rp, CamState<N> *states,
+                                                       const VertexIn<N> *vins, const int *q_in,
+                                                       const unsigned long long *cnt_in, int *q_out,
+                                                       unsigned long long *cnt_out, Queue qe, Queue ql,
+                                                       unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long n = (long long)*cnt_in;
@@ -441,7 +518,10 @@ __global__ void __launch_bounds__(kBlock) k_cam_level(DevScene sc, RenderParams 
     for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
         const int id = q_in[i];
         CamState<N> st = states[id];
-        const bool alive = camera_step<N>(sc, rp, stack, rp.path_begin + id, st, qe, ql, c);
+        const VertexIn<N> vin = vins[id];
+        const long long g = rp.path_begin + id;
+        const bool alive = kVolume ? camera_volume<N>(sc, rp, stack, g, st, vin, qe, c)
+                                   : camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c);
         ++st.level;
         states[id] = st;
         push_path(q_out, cnt_out, id, alive && st.mode != 0);

@@ -132,9 +132,10 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         const int levels = o->max_bounces + 1;  // a continuing vertex always spends one bounce
         bool wavefront = s->camera_schedule == DTRT_CAMERA_WAVEFRONT ||
                          (s->camera_schedule == DTRT_CAMERA_AUTO && Bw >= kWavefrontMinPaths);
-        if (wavefront && !(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, (size_t)Bw * sizeof(CamState<N>)) &&
-                           ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)2 * Bw * sizeof(int)) &&
-                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)(levels + 1) * sizeof(unsigned long long)))) {
+        const size_t state_bytes = ((size_t)Bw * sizeof(CamState<N>) + 255) & ~(size_t)255;
+        if (wavefront && !(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, state_bytes + (size_t)Bw * sizeof(VertexIn<N>)) &&
+                           ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)4 * Bw * sizeof(int)) &&
+                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)3 * (levels + 1) * sizeof(unsigned long long)))) {
             if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
             cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
             wavefront = false;
@@ -143,8 +144,11 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         DT_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
         used_wavefront = wavefront;
         CamState<N> *states = (CamState<N> *)sb.cam_state;
-        int *qa = (int *)sb.cam_q, *qb = qa + Bw;
-        unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt;
+        VertexIn<N> *vins = (VertexIn<N> *)((char *)sb.cam_state + state_bytes);
+        int *qa = (int *)sb.cam_q, *qb = qa + Bw, *qv = qb + Bw, *qs = qv + Bw;
+        // counts: live paths per level [0, levels], then volume and interface vertices per level
+        unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt, *vcnt = lcnt + (levels + 1),
+                           *scnt = vcnt + (levels + 1);
         for (long long b0 = 0; b0 < total; b0 += B) {
             ++batches;
             rp.path_begin = b0;
@@ -154,15 +158,21 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                 // grid-stride launches of a few waves: late levels hold few live paths
                 const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
                 if ((rc = timed(ms_camera, [&] {
-                         cudaMemsetAsync(lcnt, 0, (size_t)(levels + 1) * sizeof(unsigned long long), st);
+                         cudaMemsetAsync(lcnt, 0, (size_t)3 * (levels + 1) * sizeof(unsigned long long), st);
                          k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, lcnt, ctr);
-                         for (int L = 0; L < levels; ++L)
-                             k_cam_level<N><<<gw, kBlock, 0, st>>>(sc, rp, states, (L & 1) ? qb : qa, lcnt + L,
-                                                                   (L & 1) ? qa : qb, lcnt + L + 1, qe, ql, ctr);
+                         for (int L = 0; L < levels; ++L) {
+                             int *qin = (L & 1) ? qb : qa, *qout = (L & 1) ? qa : qb;
+                             k_cam_decide<N><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qin, lcnt + L, qv, vcnt + L,
+                                                                    qs, scnt + L, ctr);
+                             k_cam_vertex<N, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qv, vcnt + L, qout,
+                                                                          lcnt + L + 1, qe, ql, ctr);
+                             k_cam_vertex<N, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qs, scnt + L, qout,
+                                                                           lcnt + L + 1, qe, ql, ctr);
+                         }
                          k_cam_accum<N><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, sb.acc1);
                      })))
                     return rc;
-                launches += levels + 1;
+                launches += 3 * levels + 1;
             } else if ((rc = timed(ms_camera, [&] {
                             k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
                         }))) {

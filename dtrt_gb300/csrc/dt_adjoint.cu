@@ -33,8 +33,9 @@ cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const flo
 }
 
 size_t AdjWave::bytes(long long cap, int levels) {
-    return (size_t)cap * (sizeof(AdjState<1>) + 2 * sizeof(int) + sizeof(float3) + kReplayEvents * sizeof(float3)) +
-           (size_t)2 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 5 arrays
+    return (size_t)cap * (sizeof(AdjState<1>) + sizeof(VertexIn<1>) + 4 * sizeof(int) + sizeof(float3) +
+                          kReplayEvents * sizeof(float3)) +
+           (size_t)6 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 6 arrays
 }
 
 void AdjWave::carve(void *base, long long capacity, int lv) {
@@ -47,10 +48,11 @@ void AdjWave::carve(void *base, long long capacity, int lv) {
     cap = capacity;
     levels = lv;
     states = take((size_t)cap * sizeof(AdjState<1>));
-    q = (int *)take((size_t)2 * cap * sizeof(int));
+    vins = take((size_t)cap * sizeof(VertexIn<1>));
+    q = (int *)take((size_t)4 * cap * sizeof(int));
     tots = (float3 *)take((size_t)cap * sizeof(float3));
     ev = (float3 *)take((size_t)cap * kReplayEvents * sizeof(float3));
-    cnt = (unsigned long long *)take((size_t)2 * (levels + 1) * sizeof(unsigned long long));
+    cnt = (unsigned long long *)take((size_t)6 * (levels + 1) * sizeof(unsigned long long));
 }
 
 // Wavefront replay of paths [rp.path_begin, +rp.path_count) in chunks of the workspace's
@@ -63,23 +65,32 @@ cudaError_t launch_adjoint_wave(const DevScene &sc, const RenderParams &range, c
     if (levels > w.levels) return cudaErrorInvalidValue;
     auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
     AdjState<1> *states = (AdjState<1> *)w.states;
-    int *qa = w.q, *qb = w.q + w.cap;
+    VertexIn<1> *vins = (VertexIn<1> *)w.vins;
+    int *qa = w.q, *qb = qa + w.cap, *qv = qb + w.cap, *qs = qv + w.cap;
     const bool pass_b = grad != nullptr && dimg != nullptr;
     RenderParams rp = range;
     for (long long b0 = 0; b0 < range.path_count; b0 += w.cap) {
         rp.path_begin = range.path_begin + b0;
         rp.path_count = std::min(w.cap, range.path_count - b0);
         const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
-        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)2 * (levels + 1) * sizeof(unsigned long long), st);
+        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)6 * (levels + 1) * sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
         for (int pass = 0; pass < (pass_b ? 2 : 1); ++pass) {
-            unsigned long long *cnt = w.cnt + pass * (levels + 1);
-            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, cnt, dimg, w.tots, pass == 1, ctr);
-            for (int L = 0; L < levels; ++L)
-                k_adj_level<1><<<gw, kBlock, 0, st>>>(sc, rp, states, (L & 1) ? qb : qa, cnt + L, (L & 1) ? qa : qb,
-                                                     cnt + L + 1, dimg, grad, w.tots, w.ev, pass == 1, ctr);
+            const bool b = pass == 1;
+            // counts of this pass: live paths per level, then volume and interface vertices per level
+            unsigned long long *cnt = w.cnt + pass * 3 * (levels + 1), *vc = cnt + (levels + 1), *sc_ = vc + (levels + 1);
+            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, qa, cnt, dimg, w.tots, b, ctr);
+            for (int L = 0; L < levels; ++L) {
+                int *qin = (L & 1) ? qb : qa, *qout = (L & 1) ? qa : qb;
+                k_adj_decide<1><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qin, cnt + L, qv, vc + L, qs, sc_ + L, dimg,
+                                                      grad, w.tots, b, ctr);
+                k_adj_vertex<1, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qv, vc + L, qout, cnt + L + 1, dimg,
+                                                            grad, w.ev, b, ctr);
+                k_adj_vertex<1, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qs, sc_ + L, qout, cnt + L + 1, dimg,
+                                                             grad, w.ev, b, ctr);
+            }
             if (pass == 0) k_adj_totals<1><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, w.tots, img_acc);
-            if (launches) *launches += levels + 1 + (pass == 0 ? 1 : 0);
+            if (launches) *launches += 3 * levels + 1 + (pass == 0 ? 1 : 0);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

@@ -70,10 +70,28 @@ DT_D bool replay_start(const DevScene &sc, const RenderParams &rp, int *stack, l
 
 // One vertex of the replayed path (camera_step's branches, values only). Pass B scatters
 // dot(dL/dI, suffix)/spp into the voxels behind every distance-sampling factor and each
-// NEE / emitter-hit event's own weight; ev holds pass A's event values.
+// NEE / emitter-hit event's own weight; ev holds pass A's event values. In three parts as
+// the camera vertex: replay_decide (random numbers, distance sampling with its scatter),
+// then replay_volume or replay_surface.
 template <int N>
-DT_D bool replay_step(const DevScene &sc, const RenderParams &rp, int *stack, bool pass_b, float3 total, float3 gpix,
-                      AdjCtx &adj, Ctr &c, float3 *ev, AdjState<N> &st) {
+DT_D int replay_decide(const DevScene &sc, const RenderParams &rp, bool pass_b, float3 total, float3 gpix, AdjCtx &adj,
+                       Ctr &c, AdjState<N> &st, VertexIn<N> &vin) {
+    Rng &rng = st.rng;
+    const float r1a = rng.next1(), r1b = rng.next1();
+    vin.r2[0] = rng.next1(); vin.r2[1] = rng.next1(); vin.r2[2] = rng.next1(); vin.r2[3] = rng.next1();
+    vin.r3a = rng.next1(); vin.r3b = rng.next1(); vin.r3c = rng.next1();
+    vin.thr = DV<N>(mk(1.f, 1.f, 1.f));
+    vin.dir_in = st.ray.d.val();
+    if (pass_b) adj.w = dot(gpix, total - st.acc) * rp.inv_spp;  // suffix radiance of this factor
+    if (st.med >= 0 && sample_distance_ad<N>(sc, sc.media[st.med], st.ray, st.its.t, r1a, r1b, rng, vin.thr, c,
+                                             pass_b ? &adj : nullptr))
+        return (st.depth == 0 || vin.thr.is_zero()) ? 0 : 1;
+    return (!st.its.valid() || vin.thr.is_zero()) ? 0 : 2;
+}
+
+template <int N>
+DT_D bool replay_volume(const DevScene &sc, const RenderParams &rp, int *stack, bool pass_b, float3 gpix, AdjCtx &adj,
+                        Ctr &c, float3 *ev, AdjState<N> &st, const VertexIn<N> &vin) {
     Rng &rng = st.rng;
     RayAD<N> &ray = st.ray;
     ItsAD<N> &its = st.its;
@@ -81,93 +99,103 @@ DT_D bool replay_step(const DevScene &sc, const RenderParams &rp, int *stack, bo
     int &med = st.med, &depth = st.depth, &mode = st.mode, &ne = st.ne;
     const float3 zero = mk(0.f, 0.f, 0.f);
     const AdjCtx *hook = pass_b ? &adj : nullptr;
+    const float *r2 = vin.r2;
+    const float r3a = vin.r3a, r3b = vin.r3b;
+    const DV<N> &thr = vin.thr;
+    const float3 dir_in = vin.dir_in;
     bool alive = false;
-    const float r1a = rng.next1(), r1b = rng.next1();
-    float r2[4];
-    r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
-    const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
-    DV<N> thr(mk(1.f, 1.f, 1.f));
-    const float3 dir_in = ray.d.val();
-    if (pass_b) adj.w = dot(gpix, total - acc) * rp.inv_spp;  // suffix radiance of this factor
-    if (med >= 0 && sample_distance_ad<N>(sc, sc.media[med], ray, its.t, r1a, r1b, rng, thr, c, hook)) {
-        // ------------------------------------------------ volumetric vertex
-        if (depth == 0 || thr.is_zero()) return false;
-        const DevPhase &ph = sc.phases[sc.media[med].phase_id];
-        const float3 Q = cmul(P, thr.val());
-        DV<N> wo;
-        float pdf_nee;
-        if (mode & MODE_VOLUME_MAIN) {
-            const int k = ne++;
-            if (pass_b && k < kReplayEvents) {
-                const float3 e = ev[k];
-                adj.w = dot(gpix, e) * rp.inv_spp;
-                nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c,
-                                is_zero3(e, 0.f) ? nullptr : hook);
-                acc = acc + e;
-            } else {
-                const Rng saved = rng;
-                DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
-                float3 e = zero;
-                if (!v.is_zero()) {
-                    const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
-                    if (pv.v > kEps)
-                        e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
-                }
-                if (pass_b && !is_zero3(e, 0.f)) {
-                    const Rng after = rng;
-                    rng = saved;
-                    adj.w = dot(gpix, e) * rp.inv_spp;
-                    DV<N> wo2;
-                    float pdf2;
-                    nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
-                    rng = after;
-                }
-                if (!pass_b && k < kReplayEvents) ev[k] = e;
-                acc = acc + e;
+    // ------------------------------------------------ volumetric vertex
+    const DevPhase &ph = sc.phases[sc.media[med].phase_id];
+    const float3 Q = cmul(P, thr.val());
+    DV<N> wo;
+    float pdf_nee;
+    if (mode & MODE_VOLUME_MAIN) {
+        const int k = ne++;
+        if (pass_b && k < kReplayEvents) {
+            const float3 e = ev[k];
+            adj.w = dot(gpix, e) * rp.inv_spp;
+            nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c,
+                            is_zero3(e, 0.f) ? nullptr : hook);
+            acc = acc + e;
+        } else {
+            const Rng saved = rng;
+            DV<N> v = nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo, pdf_nee, c);
+            float3 e = zero;
+            if (!v.is_zero()) {
+                const Df<N> pv = phase_eval_ad<N>(ph, -ray.d, wo);
+                if (pv.v > kEps)
+                    e = cmul(Q, v.val()) * (pv.v * mis_weight(pdf_nee, phase_eval(ph, -dir_in, wo.val())));
             }
-        }
-        const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
-        if (pvs.v > kEps) {
-            const float3 thr1 = thr.val() * pvs.v;
-            ray.d = wo;
-            ItsAD<N> its1;
-            const int k = ne++;
-            if (pass_b && k < kReplayEvents) {
-                const float3 e = ev[k];
+            if (pass_b && !is_zero3(e, 0.f)) {
+                const Rng after = rng;
+                rng = saved;
                 adj.w = dot(gpix, e) * rp.inv_spp;
-                look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr, nullptr,
-                                       c, is_zero3(e, 0.f) ? nullptr : hook);
-                acc = acc + e;
-            } else {
-                const Rng saved = rng;
-                DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee,
-                                                   nullptr, nullptr, c);
-                float3 e = zero;
-                if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
-                    e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
-                if (pass_b && !is_zero3(e, 0.f)) {
-                    const Rng after = rng;
-                    rng = saved;
-                    adj.w = dot(gpix, e) * rp.inv_spp;
-                    ItsAD<N> its2;
-                    float pdf2;
-                    look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr,
-                                           c, hook);
-                    rng = after;
-                }
-                if (!pass_b && k < kReplayEvents) ev[k] = e;
-                acc = acc + e;
+                DV<N> wo2;
+                float pdf2;
+                nee_point_ad<N>(sc, stack, ray.o, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                rng = after;
             }
-            its = its1;
-            P = cmul(P, thr1);
-            depth -= 1;
-            mode &= ~MODE_EMISSION;
-            alive = true;
+            if (!pass_b && k < kReplayEvents) ev[k] = e;
+            acc = acc + e;
         }
-        return alive;
     }
+    const Df<N> pvs = phase_sample_ad<N>(ph, -ray.d, r3a, r3b, wo);
+    if (pvs.v > kEps) {
+        const float3 thr1 = thr.val() * pvs.v;
+        ray.d = wo;
+        ItsAD<N> its1;
+        const int k = ne++;
+        if (pass_b && k < kReplayEvents) {
+            const float3 e = ev[k];
+            adj.w = dot(gpix, e) * rp.inv_spp;
+            look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee, nullptr, nullptr,
+                                   c, is_zero3(e, 0.f) ? nullptr : hook);
+            acc = acc + e;
+        } else {
+            const Rng saved = rng;
+            DV<N> att = look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its1, pdf_nee,
+                                               nullptr, nullptr, c);
+            float3 e = zero;
+            if (!att.is_zero() && (mode & MODE_VOLUME_MAIN))
+                e = cmul(cmul(P, thr1), att.val()) * mis_weight(phase_eval(ph, -wo.val(), wo.val()), pdf_nee);
+            if (pass_b && !is_zero3(e, 0.f)) {
+                const Rng after = rng;
+                rng = saved;
+                adj.w = dot(gpix, e) * rp.inv_spp;
+                ItsAD<N> its2;
+                float pdf2;
+                look_for_emitter_ad<N>(sc, stack, ray, false, rng, med, depth - 1, its2, pdf2, nullptr, nullptr,
+                                       c, hook);
+                rng = after;
+            }
+            if (!pass_b && k < kReplayEvents) ev[k] = e;
+            acc = acc + e;
+        }
+        its = its1;
+        P = cmul(P, thr1);
+        depth -= 1;
+        mode &= ~MODE_EMISSION;
+        alive = true;
+    }
+    return alive;
+}
+
+template <int N>
+DT_D bool replay_surface(const DevScene &sc, const RenderParams &rp, int *stack, bool pass_b, float3 gpix,
+                         AdjCtx &adj, Ctr &c, float3 *ev, AdjState<N> &st, const VertexIn<N> &vin) {
+    Rng &rng = st.rng;
+    RayAD<N> &ray = st.ray;
+    ItsAD<N> &its = st.its;
+    float3 &P = st.P, &acc = st.acc;
+    int &med = st.med, &depth = st.depth, &mode = st.mode, &ne = st.ne;
+    const float3 zero = mk(0.f, 0.f, 0.f);
+    const AdjCtx *hook = pass_b ? &adj : nullptr;
+    const float *r2 = vin.r2;
+    const float r3a = vin.r3a, r3b = vin.r3b, r3c = vin.r3c;
+    const DV<N> &thr = vin.thr;
+    const float3 dir_in = vin.dir_in;
+    bool alive = false;
     // ---------------------------------------------------- interface vertex
-    if (!its.valid() || thr.is_zero()) return false;
     const DevShape &sh = sc.shapes[its.shape];
     if (is_transition(sh) && target_medium(sc, its.shape, its.ng, -dir_in) != med) return false;
     const float3 Q = cmul(P, thr.val());
@@ -262,6 +290,16 @@ DT_D bool replay_step(const DevScene &sc, const RenderParams &rp, int *stack, bo
 }
 
 template <int N>
+DT_D bool replay_step(const DevScene &sc, const RenderParams &rp, int *stack, bool pass_b, float3 total, float3 gpix,
+                      AdjCtx &adj, Ctr &c, float3 *ev, AdjState<N> &st) {
+    VertexIn<N> vin;
+    const int kind = replay_decide<N>(sc, rp, pass_b, total, gpix, adj, c, st, vin);
+    if (kind == 1) return replay_volume<N>(sc, rp, stack, pass_b, gpix, adj, c, ev, st, vin);
+    if (kind == 2) return replay_surface<N>(sc, rp, stack, pass_b, gpix, adj, c, ev, st, vin);
+    return false;
+}
+
+template <int N>
 DT_D float3 replay_path(const DevScene &sc, const RenderParams &rp, int *stack, long long g, bool pass_b, float3 total,
                         float3 gpix, AdjCtx &adj, Ctr &c, float3 *ev) {
     AdjState<N> st;
@@ -320,7 +358,12 @@ __global__ void __launch_bounds__(kBlock) k_adjoint(DevScene sc, RenderParams rp
 }
 
 // Wavefront schedule of the replay: pass A and pass B each run one launch per path
-// vertex over the paths still alive (compacted path-index queues, as k_cam_level).
+// vertex over the paths still alive (compacted path-index queues, as the camera stage).
+DT_D float3 pixel_dldi(const RenderParams &rp, const float *dimg, long long g) {
+    const int pixel = (int)(g / rp.spp);
+    return mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1), __ldg(dimg + 3 * (size_t)pixel + 2));
+}
+
 template <int N>
 __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams rp, AdjState<N> *states, int *q_out,
                                                       unsigned long long *cnt_out, const float *dimg,
@@ -334,10 +377,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams 
         const long long g = rp.path_begin + gi;
         bool run = true;
         if (pass_b) {  // pass B only for paths with a value whose pixel has a non-zero dL/dI
-            const int pixel = (int)(g / rp.spp);
-            const float3 gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1),
-                                 __ldg(dimg + 3 * (size_t)pixel + 2));
-            run = !is_zero3(totals[gi], 0.f) && !is_zero3(gp, 0.f);
+            run = !is_zero3(totals[gi], 0.f) && !is_zero3(pixel_dldi(rp, dimg, g), 0.f);
         }
         if (run) {
             AdjState<N> st;
@@ -349,12 +389,40 @@ __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams 
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
+// Vertex level of one pass, first part: random numbers and distance sampling (with the
+// pass-B scatter of its factor); the path is queued as a volume or an interface vertex.
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_adj_level(DevScene sc, RenderParams rp, AdjState<N> *states, const int *q_in,
-                                                      const unsigned long long *cnt_in, int *q_out,
-                                                      unsigned long long *cnt_out, const float *dimg, float *grad,
-                                                      const float3 *totals, float3 *evbuf, bool pass_b,
-                                                      unsigned long long *ctr) {
+__global__ void __launch_bounds__(kBlock) k_adj_decide(DevScene sc, RenderParams rp, AdjState<N> *states,
+                                                       VertexIn<N> *vins, const int *q_in,
+                                                       const unsigned long long *cnt_in, int *qv,
+                                                       unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s,
+                                                       const float *dimg, float *grad, const float3 *totals,
+                                                       bool pass_b, unsigned long long *ctr) {
+    const long long n = (long long)*cnt_in;
+    Ctr c;
+    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
+        const int id = q_in[i];
+        AdjState<N> st = states[id];
+        const float3 zero = mk(0.f, 0.f, 0.f);
+        const float3 total = pass_b ? totals[id] : zero, gp = pass_b ? pixel_dldi(rp, dimg, rp.path_begin + id) : zero;
+        AdjCtx adj{grad, 0.f};
+        VertexIn<N> vin;
+        const int kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
+        states[id] = st;
+        if (kind) vins[id] = vin;
+        push_path(qv, cnt_v, id, kind == 1);
+        push_path(qs, cnt_s, id, kind == 2);
+    }
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// Vertex level of one pass, second part: the volume (kVolume) or interface vertices.
+template <int N, bool kVolume>
+__global__ void __launch_bounds__(kBlock) k_adj_vertex(DevScene sc, RenderParams rp, AdjState<N> *states,
+                                                       const VertexIn<N> *vins, const int *q_in,
+                                                       const unsigned long long *cnt_in, int *q_out,
+                                                       unsigned long long *cnt_out, const float *dimg, float *grad,
+                                                       float3 *evbuf, bool pass_b, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long n = (long long)*cnt_in;
@@ -362,15 +430,12 @@ __global__ void __launch_bounds__(kBlock) k_adj_level(DevScene sc, RenderParams 
     for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
         const int id = q_in[i];
         AdjState<N> st = states[id];
-        const float3 zero = mk(0.f, 0.f, 0.f);
-        float3 total = zero, gp = zero;
-        if (pass_b) {
-            const int pixel = (int)((rp.path_begin + id) / rp.spp);
-            total = totals[id];
-            gp = mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1), __ldg(dimg + 3 * (size_t)pixel + 2));
-        }
+        const VertexIn<N> vin = vins[id];
+        const float3 gp = pass_b ? pixel_dldi(rp, dimg, rp.path_begin + id) : mk(0.f, 0.f, 0.f);
         AdjCtx adj{grad, 0.f};
-        const bool alive = replay_step<N>(sc, rp, stack, pass_b, total, gp, adj, c, evbuf + (size_t)id * kReplayEvents, st);
+        float3 *ev = evbuf + (size_t)id * kReplayEvents;
+        const bool alive = kVolume ? replay_volume<N>(sc, rp, stack, pass_b, gp, adj, c, ev, st, vin)
+                                   : replay_surface<N>(sc, rp, stack, pass_b, gp, adj, c, ev, st, vin);
         ++st.level;
         states[id] = st;
         push_path(q_out, cnt_out, id, alive && st.mode != 0);

@@ -75,10 +75,10 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
                    int on_device, cudaStream_t stream);
 cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const float *dimg, float *grad, double *img_acc,
                            unsigned long long *ctr, long long stride, cudaStream_t st);
-// Device workspace of the wavefront density replay: path states, two path-index queues,
+// Device workspace of the wavefront density replay: path states, vertex inputs, four path-index queues,
 // pass-A values and event values for `cap` paths, level counts of both passes.
 struct AdjWave {
-    void *states = nullptr;
+    void *states = nullptr, *vins = nullptr;
     int *q = nullptr;
     float3 *tots = nullptr, *ev = nullptr;
     unsigned long long *cnt = nullptr;

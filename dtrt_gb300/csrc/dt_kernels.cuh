@@ -463,20 +463,28 @@ DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = id;  // at most one push per path and level
 }
 
+// Path start and the first part of vertex level 0 (random numbers, distance sampling):
+// each path is queued as a volume or an interface vertex of level 0, or ends.
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams rp, CamState<N> *states, int *q_out,
-                                                      unsigned long long *cnt_out, unsigned long long *ctr) {
+__global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams rp, CamState<N> *states,
+                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v, int *qs,
+                                                      unsigned long long *cnt_s, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
-    bool live = false;
+    int kind = 0;
     if (gi < rp.path_count) {
         CamState<N> st;
-        live = camera_start<N>(sc, rp, stack, rp.path_begin + gi, st, c) && st.mode != 0;
+        if (camera_start<N>(sc, rp, stack, rp.path_begin + gi, st, c) && st.mode != 0) {
+            VertexIn<N> vin;
+            kind = camera_decide<N>(sc, st, vin, c);
+            if (kind) vins[gi] = vin;
+        }
         states[gi] = st;
     }
-    push_path(q_out, cnt_out, (int)gi, live);
+    push_path(qv, cnt_v, (int)gi, kind == 1);
+    push_path(qs, cnt_s, (int)gi, kind == 2);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 

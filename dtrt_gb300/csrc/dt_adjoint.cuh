@@ -364,28 +364,35 @@ DT_D float3 pixel_dldi(const RenderParams &rp, const float *dimg, long long g) {
     return mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1), __ldg(dimg + 3 * (size_t)pixel + 2));
 }
 
+// Path start and the first part of vertex level 0 of one pass; pass B starts only paths
+// with a value whose pixel has a non-zero dL/dI.
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams rp, AdjState<N> *states, int *q_out,
-                                                      unsigned long long *cnt_out, const float *dimg,
+__global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams rp, AdjState<N> *states,
+                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v, int *qs,
+                                                      unsigned long long *cnt_s, const float *dimg, float *grad,
                                                       const float3 *totals, bool pass_b, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
-    bool live = false;
+    int kind = 0;
     if (gi < rp.path_count) {
         const long long g = rp.path_begin + gi;
-        bool run = true;
-        if (pass_b) {  // pass B only for paths with a value whose pixel has a non-zero dL/dI
-            run = !is_zero3(totals[gi], 0.f) && !is_zero3(pixel_dldi(rp, dimg, g), 0.f);
-        }
-        if (run) {
+        const float3 zero = mk(0.f, 0.f, 0.f);
+        const float3 total = pass_b ? totals[gi] : zero, gp = pass_b ? pixel_dldi(rp, dimg, g) : zero;
+        if (!pass_b || (!is_zero3(total, 0.f) && !is_zero3(gp, 0.f))) {
             AdjState<N> st;
-            live = replay_start<N>(sc, rp, stack, g, st, c) && st.mode != 0;
+            if (replay_start<N>(sc, rp, stack, g, st, c) && st.mode != 0) {
+                AdjCtx adj{grad, 0.f};
+                VertexIn<N> vin;
+                kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
+                if (kind) vins[gi] = vin;
+            }
             states[gi] = st;
         }
     }
-    push_path(q_out, cnt_out, (int)gi, live);
+    push_path(qv, cnt_v, (int)gi, kind == 1);
+    push_path(qs, cnt_s, (int)gi, kind == 2);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 

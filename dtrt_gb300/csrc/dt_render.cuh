@@ -174,7 +174,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                          k_cam_accum<N><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, sb.acc1);
                      })))
                     return rc;
-                launches += 3 * levels + 1;  // start, 2 + 3 (levels - 1) level launches, accumulation
+                launches += 3 * levels + 1;  // start, 3 per level (2 at level 0), accumulation
             } else if ((rc = timed(ms_camera, [&] {
                             k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
                         }))) {

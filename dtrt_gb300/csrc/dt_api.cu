@@ -706,6 +706,7 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
                                                            tp.media_res[3 * mi + 2] != o.density.res[2]))))
             return fail("scene update: a medium changed its type or grid resolution");
     }
+    for (const DevMedium &m : media) ds.has_grid_media |= m.type == MEDIUM_HETEROGENEOUS ? 1 : 0;
     // ------------------------------------------------------------ light tables, scene.cpp:45-98
     std::vector<float> light_pmf(d->num_emitters), light_cdf(d->num_emitters), light_area(d->num_emitters), area_cdf;
     std::vector<int> area_begin(d->num_emitters);

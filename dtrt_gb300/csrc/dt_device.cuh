@@ -1130,6 +1130,25 @@ DT_HEAVY float3 look_for_emitter(const DevScene &sc, int *stack, float3 o, float
         return zero;
     }
     shape_intersect(sc, prim, o, d, its);
+    if (sc.has_grid_media) {  // geometry first: chains that miss every emitter skip transmittance
+        float3 o1 = o;
+        Its n1 = its;
+        int p1 = prim;
+        bool emitter = false;
+        for (int inter = 0; inter < kMaxInteractions; ++inter) {
+            if (inter > 0) shape_intersect(sc, p1, o1, d, n1);
+            const DevShape &s = sc.shapes[n1.shape];
+            if (s.light_id >= 0) {
+                emitter = true;
+                break;
+            }
+            if (inter == max_inter || sc.bsdfs[s.bsdf_id].type != BSDF_NULL) break;
+            o1 = o1 + d * n1.t;
+            p1 = closest_hit(sc, stack, o1, d, kShadowEps, INFINITY, th, c);
+            if (p1 < 0) break;
+        }
+        if (!emitter) return zero;
+    }
     float tr = 1.f;
     Its ni = its;
     for (int inter = 0; inter < kMaxInteractions; ++inter) {
@@ -1167,6 +1186,30 @@ DT_HEAVY DV<N> look_for_emitter_ad(const DevScene &sc, int *stack, RayAD<N> ray,
         return DV<N>();
     }
     shape_intersect_ad<N>(sc, prim, ray, its);
+    if (sc.has_grid_media) {
+        // Geometry first: follow null interfaces to the surface that ends the chain. A chain
+        // that does not end at an emitter contributes nothing, so its transmittance (a
+        // tracking estimate through the grid, with random numbers) is never evaluated. The
+        // reference evaluates it segment by segment before the emitter test
+        // (scene.cpp:660-690); the contribution is the same, its random numbers are not drawn.
+        RayAD<N> r1 = ray;
+        ItsAD<N> n1 = its;
+        int p1 = prim;
+        bool emitter = false;
+        for (int inter = 0; inter < kMaxInteractions; ++inter) {
+            if (inter > 0) shape_intersect_ad<N>(sc, p1, r1, n1);
+            const DevShape &s = sc.shapes[n1.shape];
+            if (s.light_id >= 0) {
+                emitter = true;
+                break;
+            }
+            if (inter == max_inter || sc.bsdfs[s.bsdf_id].type != BSDF_NULL) break;
+            r1.o = r1.o + r1.d * n1.t;
+            p1 = closest_hit(sc, stack, r1.o.val(), r1.d.val(), kShadowEps, INFINITY, th, c);
+            if (p1 < 0) break;
+        }
+        if (!emitter) return DV<N>();
+    }
     Df<N> tr(1.f), dist(0.f);
     ItsAD<N> ni = its;
     for (int inter = 0; inter < kMaxInteractions; ++inter) {

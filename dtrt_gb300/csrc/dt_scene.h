@@ -147,6 +147,7 @@ struct DevScene {
     DevCamera cam;
     int tracking_cap;
     int moving_geometry;           // any vertex velocity present
+    int has_grid_media;            // a heterogeneous medium exists (transmittance is a random estimate)
     unsigned est_flags;            // estimator variants, EST_* (0: the reference's estimator)
     unsigned int *error_flags;     // device flags: bit0 stack overflow, bit1 tracking cap, bit2 queue overflow
 };

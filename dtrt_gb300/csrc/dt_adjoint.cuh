@@ -38,7 +38,7 @@ constexpr int kReplayEvents = 40;
 
 // State of one replayed camera path between vertices (wavefront schedule: in HBM).
 template <int N>
-struct AdjState {
+struct alignas(16) AdjState {
     Rng rng;
     RayAD<N> ray;
     ItsAD<N> its;

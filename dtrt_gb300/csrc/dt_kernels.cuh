@@ -145,7 +145,7 @@ DT_D RayAD<N> camera_ray_ad(const DevCamera &cam, double x, double y) {
 // State of one camera path between vertices (volpathAD.cpp:145-620 as a loop): the
 // megakernel keeps it in registers, the wavefront schedule in HBM between launches.
 template <int N>
-struct CamState {
+struct alignas(16) CamState {  // 16-byte aligned: whole-state copies compile to 128-bit loads and stores
     Rng rng;
     RayAD<N> ray;
     ItsAD<N> its;
@@ -178,7 +178,7 @@ DT_D bool camera_start(const DevScene &sc, const RenderParams &rp, int *stack, l
 // Random numbers of a vertex drawn before its branch, the distance-sampling throughput and
 // the incoming direction: what the volume and interface halves of a vertex share.
 template <int N>
-struct VertexIn {
+struct alignas(16) VertexIn {
     float r2[4], r3a, r3b, r3c;
     DV<N> thr;
     float3 dir_in;

@@ -197,6 +197,7 @@ _SIGNATURES = {
     "dtrt_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDesc), ctypes.POINTER(ctypes.c_void_p)]),
     "dtrt_scene_set_edge_weights": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int]),
     "dtrt_scene_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dtrt_release_cached_memory": (ctypes.c_int, []),
     "dtrt_scene_update": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SceneDesc), ctypes.c_uint,
                                          ctypes.POINTER(UpdateStats)]),
     "dtrt_render_fwd": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptions), ctypes.c_void_p,

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -991,6 +992,38 @@ int set_edge_weights(dtrt_scene *s, const float *w) {
     return DTRT_OK;
 }
 
+void free_scratch(Scratch &b) {
+    void *ptrs[] = {b.acc1,     b.acc2,     b.out,     b.qe,     b.ql,      b.qli,       b.counts,   b.err,
+                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    b = Scratch();
+}
+
+// Render work buffers (queues of 16-24 Mi records, path states, accumulators: GBs) of the
+// last destroyed scene, kept for the next scene created on the same device: a loop that
+// builds a scene per iteration (the reference's render_scene) allocates them once.
+struct ScratchCache {
+    std::mutex mu;
+    Scratch buf;
+    int device = -1;
+    bool held = false;
+};
+ScratchCache &scratch_cache() {
+    static ScratchCache c;
+    return c;
+}
+
+void adopt_cached_scratch(dtrt_scene *s) {
+    ScratchCache &c = scratch_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    if (c.held && c.device == s->device) {
+        s->scratch = c.buf;
+        c.buf = Scratch();
+        c.held = false;
+    }
+}
+
 void free_scene(dtrt_scene *s) {
     for (void *p : s->allocs)
         if (p) cudaFree(p);
@@ -999,12 +1032,13 @@ void free_scene(dtrt_scene *s) {
     for (void *p : s->dgrid_bufs)
         if (p) cudaFree(p);
     s->dgrid_bufs.clear();
-    Scratch &b = s->scratch;
-    void *ptrs[] = {b.acc1,     b.acc2,     b.out,     b.qe,     b.ql,      b.qli,       b.counts,   b.err,
-                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt};
-    for (void *p : ptrs)
-        if (p) cudaFree(p);
-    b = Scratch();
+    ScratchCache &c = scratch_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    if (c.held) free_scratch(c.buf);
+    c.buf = s->scratch;
+    c.device = s->device;
+    c.held = true;
+    s->scratch = Scratch();
 }
 
 // re-upload the host copy of the media array after a parameter change
@@ -1066,6 +1100,7 @@ int dtrt_scene_create(const dtrt_scene_desc *desc, dtrt_scene **out) {
     std::unique_ptr<dtrt_scene> s(new dtrt_scene());
     s->nder = desc->nder;
     cudaGetDevice(&s->device);
+    dt::adopt_cached_scratch(s.get());
     dt::Builder bld(s.get());
     int st = dt::build_scene(s.get(), desc, bld, true, nullptr);
     if (st == DTRT_OK) st = dt::set_edge_weights(s.get(), desc->edge_weights);
@@ -1089,6 +1124,14 @@ int dtrt_scene_destroy(dtrt_scene *scene) {
     if (!scene) return DTRT_OK;
     dt::free_scene(scene);
     delete scene;
+    return DTRT_OK;
+}
+
+int dtrt_release_cached_memory(void) {
+    dt::ScratchCache &c = dt::scratch_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    if (c.held) dt::free_scratch(c.buf);
+    c.held = false;
     return DTRT_OK;
 }
 

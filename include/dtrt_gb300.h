@@ -218,8 +218,12 @@ int dtrt_scene_create(const dtrt_scene_desc *desc, dtrt_scene **out);
  * include/scene.h:37-39 / src/scene.cpp:138-142. */
 int dtrt_scene_set_edge_weights(dtrt_scene *scene, const float *weights, int num_shapes);
 
-/* Release every device allocation of the scene. */
+/* Release the scene's own device allocations. Its render work buffers (record queues,
+ * path states, accumulators; several GB at full size) are kept for the next scene created
+ * on the same device, so that a loop building one scene per iteration allocates them once;
+ * dtrt_release_cached_memory frees them. */
 int dtrt_scene_destroy(dtrt_scene *scene);
+int dtrt_release_cached_memory(void);
 
 /* In-place rebuild of a scene from a description with the same triangles: the same nder,
  * number of shapes, per-shape vertex and triangle counts and index lists, the same number

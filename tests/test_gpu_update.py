@@ -169,3 +169,21 @@ def test_render_scene_reuse_matches_fresh_builds(monkeypatch):
     assert sr._kept is None
     assert torch.equal(img2, fresh)
     assert not torch.equal(img1[0], img2[0])
+
+
+def test_render_buffers_pass_to_the_next_scene():
+    """A destroyed scene's render work buffers go to the next scene created on the device:
+    renders are unchanged by the reuse and by releasing the cached buffers."""
+    spec = sphere(False)
+    lib = _abi.load()
+    with native.NativeScene(spec) as a:
+        ref = a.render(seed=2, **KW)
+        ref_adj = a.render_adjoint(np.ones((64, 64, 3), np.float32), seed=2, spp=4, max_bounces=3, sppe=0)[0]
+    with native.NativeScene(spec) as b:  # takes a's buffers
+        assert np.array_equal(b.render(seed=2, **KW), ref)
+        assert np.array_equal(b.render_adjoint(np.ones((64, 64, 3), np.float32), seed=2, spp=4, max_bounces=3,
+                                               sppe=0)[0], ref_adj)
+    assert lib.dtrt_release_cached_memory() == _abi.DTRT_OK
+    assert lib.dtrt_release_cached_memory() == _abi.DTRT_OK  # nothing cached: still fine
+    with native.NativeScene(spec) as c:  # fresh buffers
+        assert np.array_equal(c.render(seed=2, **KW), ref)

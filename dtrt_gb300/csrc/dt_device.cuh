@@ -1343,68 +1343,103 @@ DT_HEAVY DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &it
 
 // ------------------------------------------------------------------ non-AD path, volpathAD.cpp:50-142
 // (the same loop is VolPathTracer::radiance, volpath.cpp:10-103, whose first hit is traced
-// from the camera: on_surface = false)
-DT_D float3 li_path(const DevScene &sc, int *stack, Rng &rng, float3 o, float3 d, int max_depth, int med,
-                    bool inc_emission, Ctr &c, bool on_surface = true) {
+// from the camera: on_surface = false). State between vertices: li_path keeps it in
+// registers, the wavefront Li schedule in HBM.
+struct alignas(16) LiState {
+    Rng rng;
     Its its;
-    float3 ret = mk(0.f, 0.f, 0.f), thr = mk(1.f, 1.f, 1.f);
-    ray_intersect(sc, stack, o, d, on_surface, its, c);
-    for (int depth = 0; depth <= max_depth; ++depth) {
-        const int max_inter = max_depth - depth - 1;
-        const float r1a = rng.next1(), r1b = rng.next1();
-        float r2[4];
-        r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
-        const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
-        const bool inside = med >= 0 && sample_distance(sc, sc.media[med], o, d, its.t, r1a, r1b, rng, thr, c);
-        if (inside) {
-            if (depth >= max_depth) break;
-            if (is_zero3(thr)) break;
-            const DevPhase &ph = sc.phases[sc.media[med].phase_id];
-            float3 wo;
-            float pdf_nee;
-            const float3 v = nee_point(sc, stack, o, r2, rng, med, max_inter, wo, pdf_nee, c);
-            if (!is_zero3(v)) {
-                const float pv = phase_eval(ph, -d, wo);
-                if (pv > kEps) ret += cmul(thr, v) * (mis_weight(pdf_nee, pv) * pv);
-            }
-            const float pv = phase_sample(ph, -d, r3a, r3b, wo);
-            if (pv < kEps) break;
-            thr = thr * pv;
-            d = wo;
-            const float3 att = look_for_emitter(sc, stack, o, d, false, rng, med, max_inter, its, pdf_nee, c);
-            if (!is_zero3(att)) ret += cmul(thr, att) * mis_weight(phase_eval(ph, -d, wo), pdf_nee);
-            inc_emission = false;
+    float3 o, d, ret, thr;
+    int med, depth, max_depth, inc_emission;
+};
+
+// First hit of the path; false when the loop would not run at all.
+DT_D bool li_start(const DevScene &sc, int *stack, LiState &s, float3 o, float3 d, int max_depth, int med,
+                   bool inc_emission, Ctr &c, bool on_surface = true) {
+    s.its = Its();
+    s.o = o;
+    s.d = d;
+    s.ret = mk(0.f, 0.f, 0.f);
+    s.thr = mk(1.f, 1.f, 1.f);
+    s.med = med;
+    s.depth = 0;
+    s.max_depth = max_depth;
+    s.inc_emission = inc_emission ? 1 : 0;
+    ray_intersect(sc, stack, o, d, on_surface, s.its, c);
+    return s.depth <= s.max_depth;
+}
+
+// One vertex (one iteration of the loop at s.depth): false when the path ends.
+DT_D bool li_step(const DevScene &sc, int *stack, LiState &s, Ctr &c) {
+    Rng &rng = s.rng;
+    Its &its = s.its;
+    float3 &o = s.o, &d = s.d, &ret = s.ret, &thr = s.thr;
+    int &med = s.med;
+    const int depth = s.depth, max_depth = s.max_depth;
+    const int max_inter = max_depth - depth - 1;
+    const float r1a = rng.next1(), r1b = rng.next1();
+    float r2[4];
+    r2[0] = rng.next1(); r2[1] = rng.next1(); r2[2] = rng.next1(); r2[3] = rng.next1();
+    const float r3a = rng.next1(), r3b = rng.next1(), r3c = rng.next1();
+    const bool inside = med >= 0 && sample_distance(sc, sc.media[med], o, d, its.t, r1a, r1b, rng, thr, c);
+    if (inside) {
+        if (depth >= max_depth) return false;
+        if (is_zero3(thr)) return false;
+        const DevPhase &ph = sc.phases[sc.media[med].phase_id];
+        float3 wo;
+        float pdf_nee;
+        const float3 v = nee_point(sc, stack, o, r2, rng, med, max_inter, wo, pdf_nee, c);
+        if (!is_zero3(v)) {
+            const float pv = phase_eval(ph, -d, wo);
+            if (pv > kEps) ret += cmul(thr, v) * (mis_weight(pdf_nee, pv) * pv);
+        }
+        const float pv = phase_sample(ph, -d, r3a, r3b, wo);
+        if (pv < kEps) return false;
+        thr = thr * pv;
+        d = wo;
+        const float3 att = look_for_emitter(sc, stack, o, d, false, rng, med, max_inter, its, pdf_nee, c);
+        if (!is_zero3(att)) ret += cmul(thr, att) * mis_weight(phase_eval(ph, -d, wo), pdf_nee);
+        s.inc_emission = 0;
+    } else {
+        if (!its.valid()) return false;
+        const DevShape &sh = sc.shapes[its.shape];
+        if (sh.light_id >= 0 && s.inc_emission) ret += cmul(thr, le(sc, its, -d));
+        if (depth >= max_depth) return false;
+        const DevBsdf &b = sc.bsdfs[sh.bsdf_id];
+        float3 wo;
+        float pdf_nee;
+        if (b.type != BSDF_NULL) {
+            const float3 v = nee_surface(sc, stack, its, r2, rng, med, max_inter, wo, pdf_nee, false, c);
+            if (!is_zero3(v))
+                ret += cmul(cmul(thr, v), bsdf_eval(b, its.wi, wo)) * mis_weight(pdf_nee, bsdf_pdf(b, its.wi, wo));
+        }
+        float bpdf, beta;
+        const float3 bw = bsdf_sample(b, its.wi, r3a, r3b, r3c, wo, bpdf, beta);
+        if (is_zero3(bw)) return false;
+        wo = its.to_world(wo);
+        o = its.p;
+        d = wo;
+        if (is_transition(sh)) med = dot(wo, its.ng) > 0.f ? sh.med_ext : sh.med_int;
+        if (b.type == BSDF_NULL) {
+            ray_intersect(sc, stack, o, d, true, its, c);
         } else {
-            if (!its.valid()) break;
-            const DevShape &s = sc.shapes[its.shape];
-            if (s.light_id >= 0 && inc_emission) ret += cmul(thr, le(sc, its, -d));
-            if (depth >= max_depth) break;
-            const DevBsdf &b = sc.bsdfs[s.bsdf_id];
-            float3 wo;
-            float pdf_nee;
-            if (b.type != BSDF_NULL) {
-                const float3 v = nee_surface(sc, stack, its, r2, rng, med, max_inter, wo, pdf_nee, false, c);
-                if (!is_zero3(v))
-                    ret += cmul(cmul(thr, v), bsdf_eval(b, its.wi, wo)) * mis_weight(pdf_nee, bsdf_pdf(b, its.wi, wo));
-            }
-            float bpdf, beta;
-            const float3 bw = bsdf_sample(b, its.wi, r3a, r3b, r3c, wo, bpdf, beta);
-            if (is_zero3(bw)) break;
-            wo = its.to_world(wo);
-            o = its.p;
-            d = wo;
-            if (is_transition(s)) med = dot(wo, its.ng) > 0.f ? s.med_ext : s.med_int;
-            if (b.type == BSDF_NULL) {
-                ray_intersect(sc, stack, o, d, true, its, c);
-                continue;
-            }
             const float3 att = look_for_emitter(sc, stack, o, d, true, rng, med, max_inter, its, pdf_nee, c);
             thr = cmul(thr, bw);
             if (!is_zero3(att, 1e-12f)) ret += cmul(thr, att) * mis_weight(bpdf, pdf_nee);
-            inc_emission = false;
+            s.inc_emission = 0;
         }
     }
-    return ret;
+    ++s.depth;
+    return s.depth <= max_depth;
+}
+
+DT_D float3 li_path(const DevScene &sc, int *stack, Rng &rng, float3 o, float3 d, int max_depth, int med,
+                    bool inc_emission, Ctr &c, bool on_surface = true) {
+    LiState s;
+    s.rng = rng;
+    bool alive = li_start(sc, stack, s, o, d, max_depth, med, inc_emission, c, on_surface);
+    while (alive) alive = li_step(sc, stack, s, c);
+    rng = s.rng;
+    return s.ret;
 }
 
 }  // namespace dt

@@ -2,9 +2,10 @@
 //
 // VolPathTracer::render (src/integrator/volpath.cpp:105-140) traces `spp` jittered
 // primary rays per pixel through VolPathTracer::radiance (volpath.cpp:10-103), which is
-// the non-AD Li loop also used by the edge terms (li_path). Here: one thread per camera
-// path, no dual numbers, no queues; per-path PCG32 streams (RndSampler(seed, path index)),
-// FP64 pixel accumulation, and the reference's unconditional write.
+// the non-AD Li loop also used by the edge terms (li_path / li_step). Here: no dual
+// numbers, no queues; per-path PCG32 streams (RndSampler(seed, path index)), FP64 pixel
+// accumulation in path order, and the reference's unconditional write. Two schedules with
+// identical results: one thread per path (k_primal) or a wavefront of li_step launches.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -44,6 +45,69 @@ __global__ void __launch_bounds__(kBlock) k_primal(DevScene sc, RenderParams rp,
         for (int k = 0; k < 3; ++k)
             if (v[k] != 0.f) atomicAdd(img_acc + (size_t)pixel * 3 + k, (double)v[k]);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+// Wavefront schedule of the primal render (as the forward camera stage): the path state
+// (LiState) between vertices in HBM, one launch per vertex over the compacted live paths,
+// each path's radiance kept per path and summed per pixel in path order.
+__global__ void __launch_bounds__(kBlock) k_primal_start(DevScene sc, RenderParams rp, LiState *states, float3 *rets,
+                                                         int *q_out, unsigned long long *cnt_out,
+                                                         unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    Ctr c;
+    bool live = false;
+    if (gi < rp.path_count) {
+        const long long g = rp.path_begin + gi;
+        const int pixel = (int)(g / rp.spp);
+        const int ix = rp.crop_x + pixel % rp.out_w, iy = rp.crop_y + pixel / rp.out_w;
+        LiState st;
+        st.rng.init(rp.seed, (uint64_t)g);
+        const double jx = st.rng.next1d(), jy = st.rng.next1d();
+        float3 o, d;
+        camera_ray(sc.cam, ix + jx, iy + jy, o, d);
+        live = li_start(sc, stack, st, o, d, rp.max_bounces, sc.cam.med_id, true, c, false);
+        if (live) states[gi] = st;
+        rets[gi] = mk(0.f, 0.f, 0.f);
+    }
+    push_path(q_out, cnt_out, (int)gi, live);
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+__global__ void __launch_bounds__(kBlock) k_primal_level(DevScene sc, RenderParams rp, LiState *states, float3 *rets,
+                                                         const int *q_in, const unsigned long long *cnt_in, int *q_out,
+                                                         unsigned long long *cnt_out, unsigned long long *ctr) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long n = (long long)*cnt_in;
+    Ctr c;
+    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
+        const int id = q_in[i];
+        LiState st = states[id];
+        const bool alive = li_step(sc, stack, st, c);
+        if (alive) states[id] = st;
+        else rets[id] = st.ret;
+        push_path(q_out, cnt_out, id, alive);
+    }
+    if (ctr) flush_counters(ctr, K_CAMERA, c);
+}
+
+__global__ void __launch_bounds__(kBlock) k_primal_accum(RenderParams rp, const float3 *rets, double *img_acc) {
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < rp.path_count;
+    const int pixel = (int)((rp.path_begin + (active ? gi : 0)) / rp.spp);
+    const float3 L = active ? rets[gi] * rp.inv_spp : mk(0.f, 0.f, 0.f);
+    const unsigned full = 0xffffffffu;
+    const int p0 = __shfl_sync(full, pixel, 0);
+    const bool uniform = __all_sync(full, active && pixel == p0);
+    float v[3] = {L.x, L.y, L.z};
+    if (uniform)
+        for (int k = 0; k < 3; ++k)
+            for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(full, v[k], off);
+    if (active && (!uniform || (threadIdx.x & 31) == 0))
+        for (int k = 0; k < 3; ++k)
+            if (v[k] != 0.f) atomicAdd(img_acc + (size_t)pixel * 3 + k, (double)v[k]);
 }
 
 __global__ void k_primal_image(int npix, const double *acc, float *out) {
@@ -95,14 +159,57 @@ int render_primal(dtrt_scene *s, const dtrt_render_options *o, float *out, int o
     DT_PCK(cudaEventCreate(&e0));
     DT_PCK(cudaEventCreate(&e1));
     const long long total = (long long)npix * o->spp;
-    const long long B = 1ll << 26;
+    long long B = 1ll << 26;  // paths per megakernel launch
     uint64_t launches = 0;
+    // schedule: AUTO runs the wavefront for large renders of scenes with grid media, whose
+    // paths differ most in length (C1 primal 42.1 -> 19.0 ms); on surface scenes the paths
+    // are short and the megakernel measured faster (C2 2.7 against 3.3 ms)
+    bool wavefront = s->camera_schedule == DTRT_CAMERA_WAVEFRONT ||
+                     (s->camera_schedule == DTRT_CAMERA_AUTO && total >= kWavefrontMinPaths && sc.has_grid_media);
+    const int levels = o->max_bounces + 2;  // li_step runs at most max_bounces + 1 vertices
+    LiState *states = nullptr;
+    float3 *rets = nullptr;
+    int *qa = nullptr, *qb = nullptr;
+    unsigned long long *lcnt = nullptr;
+    if (wavefront) {
+        B = std::min<long long>(1ll << 22, std::max<long long>(total, 1));
+        const size_t sbytes = ((size_t)B * sizeof(LiState) + 255) & ~(size_t)255;
+        if (ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, sbytes + (size_t)B * sizeof(float3)) &&
+            ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)2 * B * sizeof(int)) &&
+            ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)(levels + 1) * sizeof(unsigned long long))) {
+            states = (LiState *)sb.cam_state;
+            rets = (float3 *)((char *)sb.cam_state + sbytes);
+            qa = (int *)sb.cam_q;
+            qb = qa + B;
+            lcnt = (unsigned long long *)sb.cam_cnt;
+        } else {
+            if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
+            cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
+            wavefront = false;
+            B = 1ll << 26;
+        }
+    }
+    int sms = 0;
+    DT_PCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
     DT_PCK(cudaEventRecord(e0, st));
     for (long long b0 = 0; b0 < total; b0 += B) {
         rp.path_begin = b0;
         rp.path_count = std::min(B, total - b0);
-        k_primal<<<(unsigned)((rp.path_count + kBlock - 1) / kBlock), kBlock, 0, st>>>(sc, rp, sb.adj_img, ctr);
-        ++launches;
+        if (!wavefront) {
+            k_primal<<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, sb.adj_img, ctr);
+            ++launches;
+            DT_PCK(cudaGetLastError());
+            continue;
+        }
+        const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
+        DT_PCK(cudaMemsetAsync(lcnt, 0, (size_t)(levels + 1) * sizeof(unsigned long long), st));
+        k_primal_start<<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, rets, qa, lcnt, ctr);
+        for (int L = 0; L < levels; ++L)
+            k_primal_level<<<gw, kBlock, 0, st>>>(sc, rp, states, rets, (L & 1) ? qb : qa, lcnt + L, (L & 1) ? qa : qb,
+                                                  lcnt + L + 1, ctr);
+        k_primal_accum<<<blocks(rp.path_count), kBlock, 0, st>>>(rp, rets, sb.adj_img);
+        launches += levels + 2;
         DT_PCK(cudaGetLastError());
     }
     DT_PCK(cudaEventRecord(e1, st));
@@ -130,6 +237,7 @@ int render_primal(dtrt_scene *s, const dtrt_render_options *o, float *out, int o
     ls.kernel_launches = launches;
     ls.batches = (uint64_t)((total + B - 1) / B);
     ls.counters_enabled = ctr != nullptr;
+    ls.camera_schedule = wavefront ? DTRT_CAMERA_WAVEFRONT : DTRT_CAMERA_MEGAKERNEL;
     ls.k_rays[0] = ls.rays = hc[0];
     ls.k_node_visits[0] = ls.node_visits = hc[1];
     ls.k_tri_tests[0] = ls.tri_tests = hc[2];

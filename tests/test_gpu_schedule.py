@@ -65,3 +65,22 @@ def test_density_adjoint_wavefront_equals_megakernel():
     assert np.array_equal(ia, ib) and ia.sum() > 0
     assert np.abs(ga).max() > 0
     assert np.abs(ga - gb).max() <= 1e-4 * np.abs(ga).max()
+
+
+@pytest.mark.parametrize("name", ["c0", "c1"])
+def test_primal_wavefront_equals_megakernel(name):
+    """dtrt_render_primal under both schedules: same li_step code and random numbers per
+    path, pixel sums in path order."""
+    make, kw = CASES[name]
+    out = {}
+    with native.NativeScene(make()) as ns:
+        ns.enable_counters(True)
+        for sched in ("megakernel", "wavefront"):
+            ns.set_camera_schedule(sched)
+            img = ns.render_primal(seed=17, spp=kw["spp"], max_bounces=kw["max_bounces"])
+            out[sched] = (img, ns.last_stats())
+    (a, sa), (b, sb) = out["megakernel"], out["wavefront"]
+    assert sa["camera_schedule"] == 1 and sb["camera_schedule"] == 2
+    assert a.sum() > 0 and np.array_equal(a, b)
+    for k in ("rays", "node_visits", "tri_tests", "grid_lookups"):
+        assert sa[k] == sb[k], k

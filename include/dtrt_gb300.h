@@ -307,12 +307,15 @@ int dtrt_scene_set_queue_capacity(dtrt_scene *scene, uint64_t max_tasks);
  * returns DTRT_ERR_STEP_CAP. */
 int dtrt_scene_set_tracking_cap(dtrt_scene *scene, int max_steps);
 
-/* How forward-mode renders run the camera paths of pass 1 (integratorAD.cpp:19-98):
- * MEGAKERNEL: one thread carries its path to the end in one launch; WAVEFRONT: one launch
- * per path vertex over the paths still alive, compacted into a queue after every vertex
- * (path state in device memory between launches); AUTO picks per render. Same estimator,
- * same random numbers per path: the images agree up to FP32 rounding and the order of
- * the FP64 pixel sums. dtrt_render_fwd_noalloc always uses the megakernel. */
+/* How renders run their camera paths: the forward-mode pass 1 (integratorAD.cpp:19-98),
+ * the density adjoint's replay and the primal render. MEGAKERNEL: one thread carries its
+ * path to the end in one launch; WAVEFRONT: launches per path vertex over the paths still
+ * alive, compacted into queues after every vertex (path state in device memory between
+ * launches); AUTO picks per render (wavefront from 65,536 paths; for the primal render only
+ * in scenes with grid media). Same code and random numbers per path and pixel sums in path
+ * order: forward and primal images are identical under both, the density gradient equal up
+ * to the order of its FP32 atomic sums. dtrt_render_fwd_noalloc, the vertex adjoint and the
+ * batch's persistent schedule always use the megakernel. */
 #define DTRT_CAMERA_AUTO 0
 #define DTRT_CAMERA_MEGAKERNEL 1
 #define DTRT_CAMERA_WAVEFRONT 2

@@ -5,9 +5,12 @@
 // Every contribution is additive into the pixel with a weight known when it is spawned,
 // so the recursion flattens into task queues:
 //
-//   k_camera   one thread per camera path sample: the LiAD chain as a loop carrying a
+//   camera     the LiAD chain of a camera path sample as a loop of vertices carrying a
 //              dual prefix throughput; emits EdgeRec (surface / volume edge term) and
-//              LinsRec (Lins interface term) records instead of recursing
+//              LinsRec (Lins interface term) records instead of recursing. Megakernel
+//              k_camera (one thread per path) or wavefront k_cam_start / k_cam_decide /
+//              k_cam_vertex / k_cam_accum (one launch per vertex kind and level over the
+//              compacted live paths)
 //   k_edge     one thread per (edge record, edge sample): FP64 silhouette test and
 //              edge-point solve, the visibility gate, then two LiTask sub-paths
 //   k_lins     one thread per Lins record: the Lins estimate with its Li sub-paths

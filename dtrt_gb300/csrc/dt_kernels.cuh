@@ -466,28 +466,37 @@ DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = id;  // at most one push per path and level
 }
 
-// Path start and the first part of vertex level 0 (random numbers, distance sampling):
-// each path is queued as a volume or an interface vertex of level 0, or ends.
+// Path start and vertex level 0 up to its interface half: primary ray, first hit, the
+// level's random numbers and distance sampling; an interface vertex (every path from a
+// camera outside media) is run here too and the path queued for level 1, a volume vertex is
+// queued for level 0's volume launch.
 template <int N>
 __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams rp, CamState<N> *states,
-                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v, int *qs,
-                                                      unsigned long long *cnt_s, unsigned long long *ctr) {
+                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v,
+                                                      int *q_next, unsigned long long *cnt_next, Queue qe, Queue ql,
+                                                      unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
     int kind = 0;
+    bool next = false;
     if (gi < rp.path_count) {
+        const long long g = rp.path_begin + gi;
         CamState<N> st;
-        if (camera_start<N>(sc, rp, stack, rp.path_begin + gi, st, c) && st.mode != 0) {
+        if (camera_start<N>(sc, rp, stack, g, st, c) && st.mode != 0) {
             VertexIn<N> vin;
             kind = camera_decide<N>(sc, st, vin, c);
-            if (kind) vins[gi] = vin;
+            if (kind == 1) vins[gi] = vin;
+            if (kind == 2) {
+                next = camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c) && st.mode != 0;
+                ++st.level;
+            }
         }
         states[gi] = st;
     }
     push_path(qv, cnt_v, (int)gi, kind == 1);
-    push_path(qs, cnt_s, (int)gi, kind == 2);
+    push_path(q_next, cnt_next, (int)gi, next);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 

@@ -364,18 +364,21 @@ DT_D float3 pixel_dldi(const RenderParams &rp, const float *dimg, long long g) {
     return mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1), __ldg(dimg + 3 * (size_t)pixel + 2));
 }
 
-// Path start and the first part of vertex level 0 of one pass; pass B starts only paths
-// with a value whose pixel has a non-zero dL/dI.
+// Path start and vertex level 0 up to its interface half, as k_cam_start: an interface
+// vertex runs here and the path is queued for level 1, a volume vertex for level 0's volume
+// launch. Pass B starts only paths with a value whose pixel has a non-zero dL/dI.
 template <int N>
 __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams rp, AdjState<N> *states,
-                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v, int *qs,
-                                                      unsigned long long *cnt_s, const float *dimg, float *grad,
-                                                      const float3 *totals, bool pass_b, unsigned long long *ctr) {
+                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v,
+                                                      int *q_next, unsigned long long *cnt_next, const float *dimg,
+                                                      float *grad, const float3 *totals, float3 *evbuf, bool pass_b,
+                                                      unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
     int kind = 0;
+    bool next = false;
     if (gi < rp.path_count) {
         const long long g = rp.path_begin + gi;
         const float3 zero = mk(0.f, 0.f, 0.f);
@@ -386,13 +389,19 @@ __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams 
                 AdjCtx adj{grad, 0.f};
                 VertexIn<N> vin;
                 kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
-                if (kind) vins[gi] = vin;
+                if (kind == 1) vins[gi] = vin;
+                if (kind == 2) {
+                    next = replay_surface<N>(sc, rp, stack, pass_b, gp, adj, c, evbuf + (size_t)gi * kReplayEvents, st,
+                                             vin) &&
+                           st.mode != 0;
+                    ++st.level;
+                }
             }
             states[gi] = st;
         }
     }
     push_path(qv, cnt_v, (int)gi, kind == 1);
-    push_path(qs, cnt_s, (int)gi, kind == 2);
+    push_path(q_next, cnt_next, (int)gi, next);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 

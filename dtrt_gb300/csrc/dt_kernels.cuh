@@ -8,9 +8,9 @@
 //   camera     the LiAD chain of a camera path sample as a loop of vertices carrying a
 //              dual prefix throughput; emits EdgeRec (surface / volume edge term) and
 //              LinsRec (Lins interface term) records instead of recursing. Megakernel
-//              k_camera (one thread per path) or wavefront k_cam_start / k_cam_decide /
-//              k_cam_vertex / k_cam_accum (one launch per vertex kind and level over the
-//              compacted live paths)
+//              k_camera (one thread per path) or wavefront k_cam_start / k_cam_vertex /
+//              k_cam_accum (one launch per vertex kind and level over the compacted paths
+//              of that kind, each ending with the next level's distance sampling)
 //   k_edge     one thread per (edge record, edge sample): FP64 silhouette test and
 //              edge-point solve, the visibility gate, then two LiTask sub-paths
 //   k_lins     one thread per Lins record: the Lins estimate with its Li sub-paths
@@ -466,70 +466,63 @@ DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = id;  // at most one push per path and level
 }
 
-// Path start and vertex level 0 up to its interface half: primary ray, first hit, the
-// level's random numbers and distance sampling; an interface vertex (every path from a
-// camera outside media) is run here too and the path queued for level 1, a volume vertex is
-// queued for level 0's volume launch.
+// After a vertex of level L: a continuing path draws the random numbers and samples the
+// distance of level L+1 right away and is queued as a volume or interface vertex of L+1.
+template <int N>
+DT_D void camera_next(const DevScene &sc, CamState<N> &st, bool alive, VertexIn<N> *vins, int id, int *qv,
+                      unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, Ctr &c) {
+    int kind = 0;
+    if (alive && st.mode != 0) {
+        VertexIn<N> vin;
+        kind = camera_decide<N>(sc, st, vin, c);
+        if (kind) vins[id] = vin;
+    }
+    push_path(qv, cnt_v, id, kind == 1);
+    push_path(qs, cnt_s, id, kind == 2);
+}
+
+// Path start and level 0: primary ray, first hit, the level's random numbers and distance
+// sampling. An interface vertex (every path from a camera outside media) runs here too and
+// the path goes on to level 1's distance sampling; a volume vertex is queued for level 0.
 template <int N>
 __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams rp, CamState<N> *states,
-                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v,
-                                                      int *q_next, unsigned long long *cnt_next, Queue qe, Queue ql,
+                                                      VertexIn<N> *vins, int *qv0, unsigned long long *cnt_v0,
+                                                      int *qv1, unsigned long long *cnt_v1, int *qs1,
+                                                      unsigned long long *cnt_s1, Queue qe, Queue ql,
                                                       unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
     int kind = 0;
+    CamState<N> st;
     bool next = false;
     if (gi < rp.path_count) {
         const long long g = rp.path_begin + gi;
-        CamState<N> st;
         if (camera_start<N>(sc, rp, stack, g, st, c) && st.mode != 0) {
             VertexIn<N> vin;
             kind = camera_decide<N>(sc, st, vin, c);
             if (kind == 1) vins[gi] = vin;
             if (kind == 2) {
-                next = camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c) && st.mode != 0;
+                next = camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c);
                 ++st.level;
             }
         }
-        states[gi] = st;
     }
-    push_path(qv, cnt_v, (int)gi, kind == 1);
-    push_path(q_next, cnt_next, (int)gi, next);
+    push_path(qv0, cnt_v0, (int)gi, kind == 1);
+    camera_next<N>(sc, st, next, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    if (gi < rp.path_count) states[gi] = st;
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
-// Vertex level L, first part: random numbers and distance sampling of every live path,
-// which is then queued as a volume or an interface vertex (or ends).
-template <int N>
-__global__ void __launch_bounds__(kBlock) k_cam_decide(DevScene sc, RenderParams rp, CamState<N> *states,
-                                                       VertexIn<N> *vins, const int *q_in,
-                                                       const unsigned long long *cnt_in, int *qv,
-                                                       unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s,
-                                                       unsigned long long *ctr) {
-    const long long n = (long long)*cnt_in;
-    Ctr c;
-    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
-        const int id = q_in[i];
-        CamState<N> st = states[id];
-        VertexIn<N> vin;
-        const int kind = camera_decide<N>(sc, st, vin, c);
-        states[id] = st;
-        if (kind) vins[id] = vin;
-        push_path(qv, cnt_v, id, kind == 1);
-        push_path(qs, cnt_s, id, kind == 2);
-    }
-    if (ctr) flush_counters(ctr, K_CAMERA, c);
-}
-
-// Vertex level L, second part: the volume (kVolume) or interface vertices of the level;
-// continuing paths go to the queue of level L+1.
+// Vertex level L, one launch per kind: the volume (kVolume) or interface vertices of the
+// level; a continuing path then runs level L+1's distance sampling (camera_next).
 template <int N, bool kVolume>
 __global__ void __launch_bounds__(kBlock) k_cam_vertex(DevScene sc, RenderParams rp, CamState<N> *states,
-                                                       const VertexIn<N> *vins, const int *q_in,
-                                                       const unsigned long long *cnt_in, int *q_out,
-                                                       unsigned long long *cnt_out, Queue qe, Queue ql,
+                                                       VertexIn<N> *vins, const int *q_in,
+                                                       const unsigned long long *cnt_in, int *qv_next,
+                                                       unsigned long long *cnt_v_next, int *qs_next,
+                                                       unsigned long long *cnt_s_next, Queue qe, Queue ql,
                                                        unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
@@ -543,8 +536,8 @@ __global__ void __launch_bounds__(kBlock) k_cam_vertex(DevScene sc, RenderParams
         const bool alive = kVolume ? camera_volume<N>(sc, rp, stack, g, st, vin, qe, c)
                                    : camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c);
         ++st.level;
+        camera_next<N>(sc, st, alive, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next, c);
         states[id] = st;
-        push_path(q_out, cnt_out, id, alive && st.mode != 0);
     }
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }

@@ -159,23 +159,23 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                 const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
                 if ((rc = timed(ms_camera, [&] {
                          cudaMemsetAsync(lcnt, 0, (size_t)3 * (levels + 1) * sizeof(unsigned long long), st);
-                         k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qv, vcnt, qb,
-                                                                                  lcnt + 1, qe, ql, ctr);
+                         // volume / interface queues of level L: (qa, qb) for even L, (qv, qs) for odd L
+                         k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qa, vcnt, qv,
+                                                                                  vcnt + 1, qs, scnt + 1, qe, ql, ctr);
                          for (int L = 0; L < levels; ++L) {
-                             int *qin = (L & 1) ? qb : qa, *qout = (L & 1) ? qa : qb;
-                             if (L > 0)  // level 0's distance sampling and interface vertices ran in k_cam_start
-                                 k_cam_decide<N><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qin, lcnt + L, qv, vcnt + L,
-                                                                        qs, scnt + L, ctr);
-                             k_cam_vertex<N, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qv, vcnt + L, qout,
-                                                                          lcnt + L + 1, qe, ql, ctr);
-                             if (L > 0)
-                                 k_cam_vertex<N, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qs, scnt + L, qout,
-                                                                               lcnt + L + 1, qe, ql, ctr);
+                             int *qvl = (L & 1) ? qv : qa, *qsl = (L & 1) ? qs : qb;
+                             int *qvn = (L & 1) ? qa : qv, *qsn = (L & 1) ? qb : qs;
+                             k_cam_vertex<N, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qvl, vcnt + L, qvn,
+                                                                          vcnt + L + 1, qsn, scnt + L + 1, qe, ql, ctr);
+                             if (L > 0)  // level 0's interface vertices ran in k_cam_start
+                                 k_cam_vertex<N, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qsl, scnt + L, qvn,
+                                                                               vcnt + L + 1, qsn, scnt + L + 1, qe, ql,
+                                                                               ctr);
                          }
                          k_cam_accum<N><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, sb.acc1);
                      })))
                     return rc;
-                launches += 3 * levels;  // start, 3 per level (1 at level 0), accumulation
+                launches += 2 * levels + 1;  // start, 2 per level (1 at level 0), accumulation
             } else if ((rc = timed(ms_camera, [&] {
                             k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
                         }))) {

@@ -79,21 +79,20 @@ cudaError_t launch_adjoint_wave(const DevScene &sc, const RenderParams &range, c
             const bool b = pass == 1;
             // counts of this pass: live paths per level, then volume and interface vertices per level
             unsigned long long *cnt = w.cnt + pass * 3 * (levels + 1), *vc = cnt + (levels + 1), *sc_ = vc + (levels + 1);
-            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qv, vc, qb, cnt + 1, dimg,
-                                                                    grad, w.tots, w.ev, b, ctr);
+            // volume / interface queues of level L: (qa, qb) for even L, (qv, qs) for odd L
+            k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qa, vc, qv, vc + 1, qs,
+                                                                    sc_ + 1, dimg, grad, w.tots, w.ev, b, ctr);
             for (int L = 0; L < levels; ++L) {
-                int *qin = (L & 1) ? qb : qa, *qout = (L & 1) ? qa : qb;
-                if (L > 0)  // level 0's distance sampling and interface vertices ran in k_adj_start
-                    k_adj_decide<1><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qin, cnt + L, qv, vc + L, qs, sc_ + L,
-                                                          dimg, grad, w.tots, b, ctr);
-                k_adj_vertex<1, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qv, vc + L, qout, cnt + L + 1, dimg,
-                                                            grad, w.ev, b, ctr);
-                if (L > 0)
-                    k_adj_vertex<1, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qs, sc_ + L, qout, cnt + L + 1,
-                                                                 dimg, grad, w.ev, b, ctr);
+                int *qvl = (L & 1) ? qv : qa, *qsl = (L & 1) ? qs : qb;
+                int *qvn = (L & 1) ? qa : qv, *qsn = (L & 1) ? qb : qs;
+                k_adj_vertex<1, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qvl, vc + L, qvn, vc + L + 1, qsn,
+                                                            sc_ + L + 1, dimg, grad, w.tots, w.ev, b, ctr);
+                if (L > 0)  // level 0's interface vertices ran in k_adj_start
+                    k_adj_vertex<1, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qsl, sc_ + L, qvn, vc + L + 1,
+                                                                 qsn, sc_ + L + 1, dimg, grad, w.tots, w.ev, b, ctr);
             }
             if (pass == 0) k_adj_totals<1><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, w.tots, img_acc);
-            if (launches) *launches += 3 * levels - 1 + (pass == 0 ? 1 : 0);  // start, 3 per level (1 at level 0), totals in pass A
+            if (launches) *launches += 2 * levels + (pass == 0 ? 1 : 0);  // start, 2 per level (1 at level 0), totals in pass A
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

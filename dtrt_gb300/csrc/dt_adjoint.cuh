@@ -364,81 +364,76 @@ DT_D float3 pixel_dldi(const RenderParams &rp, const float *dimg, long long g) {
     return mk(__ldg(dimg + 3 * (size_t)pixel), __ldg(dimg + 3 * (size_t)pixel + 1), __ldg(dimg + 3 * (size_t)pixel + 2));
 }
 
-// Path start and vertex level 0 up to its interface half, as k_cam_start: an interface
-// vertex runs here and the path is queued for level 1, a volume vertex for level 0's volume
-// launch. Pass B starts only paths with a value whose pixel has a non-zero dL/dI.
+// After a vertex of level L of one pass: a continuing path runs level L+1's random numbers
+// and distance sampling (with pass B's scatter of its factor) and is queued as a volume or
+// interface vertex of L+1 (as camera_next).
+template <int N>
+DT_D void replay_next(const DevScene &sc, const RenderParams &rp, AdjState<N> &st, bool alive, bool pass_b,
+                      float3 total, float3 gp, AdjCtx &adj, VertexIn<N> *vins, int id, int *qv,
+                      unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, Ctr &c) {
+    int kind = 0;
+    if (alive && st.mode != 0) {
+        VertexIn<N> vin;
+        kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
+        if (kind) vins[id] = vin;
+    }
+    push_path(qv, cnt_v, id, kind == 1);
+    push_path(qs, cnt_s, id, kind == 2);
+}
+
+// Path start and level 0 of one pass, as k_cam_start: an interface vertex runs here and
+// the path goes on to level 1's distance sampling, a volume vertex is queued for level 0.
+// Pass B starts only paths with a value whose pixel has a non-zero dL/dI.
 template <int N>
 __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams rp, AdjState<N> *states,
-                                                      VertexIn<N> *vins, int *qv, unsigned long long *cnt_v,
-                                                      int *q_next, unsigned long long *cnt_next, const float *dimg,
-                                                      float *grad, const float3 *totals, float3 *evbuf, bool pass_b,
+                                                      VertexIn<N> *vins, int *qv0, unsigned long long *cnt_v0,
+                                                      int *qv1, unsigned long long *cnt_v1, int *qs1,
+                                                      unsigned long long *cnt_s1, const float *dimg, float *grad,
+                                                      const float3 *totals, float3 *evbuf, bool pass_b,
                                                       unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
     int kind = 0;
-    bool next = false;
+    bool next = false, run = false;
+    AdjState<N> st;
+    const float3 zero = mk(0.f, 0.f, 0.f);
+    float3 total = zero, gp = zero;
+    AdjCtx adj{grad, 0.f};
     if (gi < rp.path_count) {
         const long long g = rp.path_begin + gi;
-        const float3 zero = mk(0.f, 0.f, 0.f);
-        const float3 total = pass_b ? totals[gi] : zero, gp = pass_b ? pixel_dldi(rp, dimg, g) : zero;
-        if (!pass_b || (!is_zero3(total, 0.f) && !is_zero3(gp, 0.f))) {
-            AdjState<N> st;
-            if (replay_start<N>(sc, rp, stack, g, st, c) && st.mode != 0) {
-                AdjCtx adj{grad, 0.f};
-                VertexIn<N> vin;
-                kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
-                if (kind == 1) vins[gi] = vin;
-                if (kind == 2) {
-                    next = replay_surface<N>(sc, rp, stack, pass_b, gp, adj, c, evbuf + (size_t)gi * kReplayEvents, st,
-                                             vin) &&
-                           st.mode != 0;
-                    ++st.level;
-                }
+        if (pass_b) {
+            total = totals[gi];
+            gp = pixel_dldi(rp, dimg, g);
+        }
+        run = !pass_b || (!is_zero3(total, 0.f) && !is_zero3(gp, 0.f));
+        if (run && replay_start<N>(sc, rp, stack, g, st, c) && st.mode != 0) {
+            VertexIn<N> vin;
+            kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
+            if (kind == 1) vins[gi] = vin;
+            if (kind == 2) {
+                next = replay_surface<N>(sc, rp, stack, pass_b, gp, adj, c, evbuf + (size_t)gi * kReplayEvents, st, vin);
+                ++st.level;
             }
-            states[gi] = st;
         }
     }
-    push_path(qv, cnt_v, (int)gi, kind == 1);
-    push_path(q_next, cnt_next, (int)gi, next);
+    push_path(qv0, cnt_v0, (int)gi, kind == 1);
+    replay_next<N>(sc, rp, st, next, pass_b, total, gp, adj, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    if (run) states[gi] = st;
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
-// Vertex level of one pass, first part: random numbers and distance sampling (with the
-// pass-B scatter of its factor); the path is queued as a volume or an interface vertex.
-template <int N>
-__global__ void __launch_bounds__(kBlock) k_adj_decide(DevScene sc, RenderParams rp, AdjState<N> *states,
-                                                       VertexIn<N> *vins, const int *q_in,
-                                                       const unsigned long long *cnt_in, int *qv,
-                                                       unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s,
-                                                       const float *dimg, float *grad, const float3 *totals,
-                                                       bool pass_b, unsigned long long *ctr) {
-    const long long n = (long long)*cnt_in;
-    Ctr c;
-    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
-        const int id = q_in[i];
-        AdjState<N> st = states[id];
-        const float3 zero = mk(0.f, 0.f, 0.f);
-        const float3 total = pass_b ? totals[id] : zero, gp = pass_b ? pixel_dldi(rp, dimg, rp.path_begin + id) : zero;
-        AdjCtx adj{grad, 0.f};
-        VertexIn<N> vin;
-        const int kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
-        states[id] = st;
-        if (kind) vins[id] = vin;
-        push_path(qv, cnt_v, id, kind == 1);
-        push_path(qs, cnt_s, id, kind == 2);
-    }
-    if (ctr) flush_counters(ctr, K_CAMERA, c);
-}
-
-// Vertex level of one pass, second part: the volume (kVolume) or interface vertices.
+// Vertex level of one pass: the volume (kVolume) or interface vertices, each continuing path
+// then running level L+1's distance sampling (replay_next).
 template <int N, bool kVolume>
 __global__ void __launch_bounds__(kBlock) k_adj_vertex(DevScene sc, RenderParams rp, AdjState<N> *states,
-                                                       const VertexIn<N> *vins, const int *q_in,
-                                                       const unsigned long long *cnt_in, int *q_out,
-                                                       unsigned long long *cnt_out, const float *dimg, float *grad,
-                                                       float3 *evbuf, bool pass_b, unsigned long long *ctr) {
+                                                       VertexIn<N> *vins, const int *q_in,
+                                                       const unsigned long long *cnt_in, int *qv_next,
+                                                       unsigned long long *cnt_v_next, int *qs_next,
+                                                       unsigned long long *cnt_s_next, const float *dimg, float *grad,
+                                                       const float3 *totals, float3 *evbuf, bool pass_b,
+                                                       unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long n = (long long)*cnt_in;
@@ -447,14 +442,15 @@ __global__ void __launch_bounds__(kBlock) k_adj_vertex(DevScene sc, RenderParams
         const int id = q_in[i];
         AdjState<N> st = states[id];
         const VertexIn<N> vin = vins[id];
-        const float3 gp = pass_b ? pixel_dldi(rp, dimg, rp.path_begin + id) : mk(0.f, 0.f, 0.f);
+        const float3 zero = mk(0.f, 0.f, 0.f);
+        const float3 total = pass_b ? totals[id] : zero, gp = pass_b ? pixel_dldi(rp, dimg, rp.path_begin + id) : zero;
         AdjCtx adj{grad, 0.f};
         float3 *ev = evbuf + (size_t)id * kReplayEvents;
         const bool alive = kVolume ? replay_volume<N>(sc, rp, stack, pass_b, gp, adj, c, ev, st, vin)
                                    : replay_surface<N>(sc, rp, stack, pass_b, gp, adj, c, ev, st, vin);
         ++st.level;
+        replay_next<N>(sc, rp, st, alive, pass_b, total, gp, adj, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next, c);
         states[id] = st;
-        push_path(q_out, cnt_out, id, alive && st.mode != 0);
     }
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }

@@ -266,8 +266,8 @@ def run_gpu(args, wl_name, rank, world, local_rank):
             traffic = t["dram_bytes_per_path"] * paths_per_step
     kname = f"k_{dom}"
     if dom == "camera" and cstats.get("camera_schedule") == 2:
-        kname = ("k_cam_vertex (camera stage: k_cam_start, then per vertex level k_cam_decide and "
-                 "k_cam_vertex for volume and interface vertices, k_cam_accum)")
+        kname = ("k_cam_vertex (camera stage: k_cam_start, then per vertex level k_cam_vertex for the "
+                 "volume and the interface vertices, k_cam_accum)")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": kname,
                 "peak_source": "measured" if peaks else "fallback",

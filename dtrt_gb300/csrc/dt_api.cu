@@ -1000,6 +1000,11 @@ void free_scratch(Scratch &b) {
     b = Scratch();
 }
 
+size_t scratch_bytes(const Scratch &b) {
+    return b.acc1_n + b.acc2_n + b.out_n + b.qe_bytes + b.ql_bytes + b.qli_bytes + b.adj_dimg_n + b.adj_grad_n +
+           b.adj_out_n + b.adj_img_n + b.cam_state_bytes + b.cam_q_bytes + b.cam_cnt_bytes;
+}
+
 // Render work buffers (queues of 16-24 Mi records, path states, accumulators: GBs) of the
 // last destroyed scene, kept for the next scene created on the same device: a loop that
 // builds a scene per iteration (the reference's render_scene) allocates them once.
@@ -1032,13 +1037,20 @@ void free_scene(dtrt_scene *s) {
     for (void *p : s->dgrid_bufs)
         if (p) cudaFree(p);
     s->dgrid_bufs.clear();
+    // keep the larger of the cached and the destroyed scene's buffers (a scene that never
+    // rendered has none)
     ScratchCache &c = scratch_cache();
     std::lock_guard<std::mutex> lock(c.mu);
-    if (c.held) free_scratch(c.buf);
-    c.buf = s->scratch;
-    c.device = s->device;
-    c.held = true;
-    s->scratch = Scratch();
+    Scratch &b = s->scratch;
+    if (!c.held || scratch_bytes(b) > scratch_bytes(c.buf) || c.device != s->device) {
+        if (c.held) free_scratch(c.buf);
+        c.buf = b;
+        c.device = s->device;
+        c.held = true;
+    } else {
+        free_scratch(b);
+    }
+    b = Scratch();
 }
 
 // re-upload the host copy of the media array after a parameter change

@@ -35,7 +35,7 @@ cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const flo
 size_t AdjWave::bytes(long long cap, int levels) {
     return (size_t)cap * (sizeof(AdjState<1>) + sizeof(VertexIn<1>) + 4 * sizeof(int) + sizeof(float3) +
                           kReplayEvents * sizeof(float3)) +
-           (size_t)6 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 6 arrays
+           (size_t)4 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 6 arrays
 }
 
 void AdjWave::carve(void *base, long long capacity, int lv) {
@@ -52,7 +52,7 @@ void AdjWave::carve(void *base, long long capacity, int lv) {
     q = (int *)take((size_t)4 * cap * sizeof(int));
     tots = (float3 *)take((size_t)cap * sizeof(float3));
     ev = (float3 *)take((size_t)cap * kReplayEvents * sizeof(float3));
-    cnt = (unsigned long long *)take((size_t)6 * (levels + 1) * sizeof(unsigned long long));
+    cnt = (unsigned long long *)take((size_t)4 * (levels + 1) * sizeof(unsigned long long));
 }
 
 // Wavefront replay of paths [rp.path_begin, +rp.path_count) in chunks of the workspace's
@@ -73,12 +73,12 @@ cudaError_t launch_adjoint_wave(const DevScene &sc, const RenderParams &range, c
         rp.path_begin = range.path_begin + b0;
         rp.path_count = std::min(w.cap, range.path_count - b0);
         const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
-        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)6 * (levels + 1) * sizeof(unsigned long long), st);
+        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)4 * (levels + 1) * sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
         for (int pass = 0; pass < (pass_b ? 2 : 1); ++pass) {
             const bool b = pass == 1;
-            // counts of this pass: live paths per level, then volume and interface vertices per level
-            unsigned long long *cnt = w.cnt + pass * 3 * (levels + 1), *vc = cnt + (levels + 1), *sc_ = vc + (levels + 1);
+            // counts of this pass: volume and interface vertices queued per level [0, levels]
+            unsigned long long *vc = w.cnt + pass * 2 * (levels + 1), *sc_ = vc + (levels + 1);
             // volume / interface queues of level L: (qa, qb) for even L, (qv, qs) for odd L
             k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qa, vc, qv, vc + 1, qs,
                                                                     sc_ + 1, dimg, grad, w.tots, w.ev, b, ctr);

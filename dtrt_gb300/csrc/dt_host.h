@@ -25,7 +25,7 @@ struct Scratch {
     float *adj_dimg = nullptr, *adj_grad = nullptr, *adj_out = nullptr;
     double *adj_img = nullptr;
     size_t adj_dimg_n = 0, adj_grad_n = 0, adj_out_n = 0, adj_img_n = 0;
-    // wavefront camera schedule: per-path state, two path-index queues, per-level counts
+    // wavefront schedules: path states and vertex inputs, four path-index queues, per-level counts
     void *cam_state = nullptr, *cam_q = nullptr, *cam_cnt = nullptr;
     size_t cam_state_bytes = 0, cam_q_bytes = 0, cam_cnt_bytes = 0;
 

@@ -127,7 +127,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         long long B = (long long)(rec_cap / (uint64_t)std::max(1, o->max_bounces + 1));
         B = std::max<long long>(unit, (B / unit) * unit);
         const long long per_chunk = std::max<long long>(1, (long long)(li_cap / (uint64_t)std::max(1, 2 * rp.sppse)));
-        // camera schedule: the wavefront keeps CamState per path of a batch in device memory
+        // camera schedule: the wavefront keeps CamState and VertexIn per path of a batch in device memory
         const long long Bw = std::min<long long>(B, total);
         const int levels = o->max_bounces + 1;  // a continuing vertex always spends one bounce
         bool wavefront = s->camera_schedule == DTRT_CAMERA_WAVEFRONT ||
@@ -135,7 +135,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         const size_t state_bytes = ((size_t)Bw * sizeof(CamState<N>) + 255) & ~(size_t)255;
         if (wavefront && !(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, state_bytes + (size_t)Bw * sizeof(VertexIn<N>)) &&
                            ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)4 * Bw * sizeof(int)) &&
-                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)3 * (levels + 1) * sizeof(unsigned long long)))) {
+                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)2 * (levels + 1) * sizeof(unsigned long long)))) {
             if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
             cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
             wavefront = false;
@@ -146,9 +146,8 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         CamState<N> *states = (CamState<N> *)sb.cam_state;
         VertexIn<N> *vins = (VertexIn<N> *)((char *)sb.cam_state + state_bytes);
         int *qa = (int *)sb.cam_q, *qb = qa + Bw, *qv = qb + Bw, *qs = qv + Bw;
-        // counts: live paths per level [0, levels], then volume and interface vertices per level
-        unsigned long long *lcnt = (unsigned long long *)sb.cam_cnt, *vcnt = lcnt + (levels + 1),
-                           *scnt = vcnt + (levels + 1);
+        // volume and interface vertices queued per level [0, levels]
+        unsigned long long *vcnt = (unsigned long long *)sb.cam_cnt, *scnt = vcnt + (levels + 1);
         for (long long b0 = 0; b0 < total; b0 += B) {
             ++batches;
             rp.path_begin = b0;
@@ -158,7 +157,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                 // grid-stride launches of a few waves: late levels hold few live paths
                 const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
                 if ((rc = timed(ms_camera, [&] {
-                         cudaMemsetAsync(lcnt, 0, (size_t)3 * (levels + 1) * sizeof(unsigned long long), st);
+                         cudaMemsetAsync(vcnt, 0, (size_t)2 * (levels + 1) * sizeof(unsigned long long), st);
                          // volume / interface queues of level L: (qa, qb) for even L, (qv, qs) for odd L
                          k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qa, vcnt, qv,
                                                                                   vcnt + 1, qs, scnt + 1, qe, ql, ctr);

@@ -72,20 +72,33 @@ struct Builder {
         }
         out.max_depth = std::max(out.max_depth, depth);
         if (count <= kLeafPref || (depth >= kDepthCap && count <= kLeafMax)) return make_leaf(first, count);
-        // binned SAH over the centroid bounds
+        // binned SAH over the centroid bounds: one pass bins all three axes
         int best_axis = -1, best_split = -1;
         float best_cost = FLT_MAX;
+        Box bins[3][kBins];
+        int counts[3][kBins] = {{0}};
+        float kb[3];
+        bool axis_ok[3];
         for (int a = 0; a < 3; ++a) {
             const float ext = cb.hi[a] - cb.lo[a];
-            if (!(ext > 0.f)) continue;
-            Box bb[kBins];
-            int bc[kBins] = {0};
-            const float k = kBins / ext;
-            for (int i = first; i < first + count; ++i) {
-                int b = std::min(kBins - 1, (int)((cen[3 * order[i] + a] - cb.lo[a]) * k));
-                bc[b]++;
-                bb[b].grow(tbox[order[i]]);
+            axis_ok[a] = ext > 0.f;
+            kb[a] = axis_ok[a] ? kBins / ext : 0.f;
+        }
+        for (int i = first; i < first + count; ++i) {
+            const int t = order[i];
+            const Box &tb = tbox[t];
+            const float *c = &cen[3 * t];
+            for (int a = 0; a < 3; ++a) {
+                if (!axis_ok[a]) continue;
+                const int b = std::min(kBins - 1, (int)((c[a] - cb.lo[a]) * kb[a]));
+                counts[a][b]++;
+                bins[a][b].grow(tb);
             }
+        }
+        for (int a = 0; a < 3; ++a) {
+            if (!axis_ok[a]) continue;
+            const Box *bb = bins[a];
+            const int *bc = counts[a];
             Box lb[kBins], rb[kBins];
             int lc[kBins], rc[kBins];
             Box acc;

@@ -12,7 +12,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -508,22 +507,31 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
     if (!cached) {  // edge adjacency from the triangle lists: sorted unique vertex pairs and their faces
         tp.adj.clear();
         tp.adj_off.assign(1, 0);
+        // each triangle side as (sorted vertex pair, face), stably sorted by the pair: the runs
+        // are the edges in increasing (a, b) order, their faces in triangle order
+        std::vector<std::pair<uint64_t, int>> he;
         for (int si = 0; si < d->num_shapes; ++si) {
             const DevShape &sh = shapes[si];
-            std::map<std::pair<int, int>, std::vector<int>> m;
+            he.resize(3 * (size_t)sh.nt);
             for (int t = 0; t < sh.nt; ++t) {
                 const int4 tr = tris[sh.tri_off + t];
                 const int ids[3] = {tr.x - sh.vert_off, tr.y - sh.vert_off, tr.z - sh.vert_off};
                 for (int e = 0; e < 3; ++e) {
-                    int a = ids[e], b = ids[(e + 1) % 3];
-                    m[a < b ? std::make_pair(a, b) : std::make_pair(b, a)].push_back(t);
+                    const int a = std::min(ids[e], ids[(e + 1) % 3]), b = std::max(ids[e], ids[(e + 1) % 3]);
+                    he[3 * (size_t)t + e] = {((uint64_t)(uint32_t)a << 32) | (uint32_t)b, t};
                 }
             }
-            for (auto const &kv : m) {
-                if (kv.second.size() > 2) return fail("non-manifold mesh: an edge is shared by more than 2 faces");
-                if (kv.second.size() == 2 && kv.second[0] == kv.second[1]) return fail("duplicated faces");
-                tp.adj.push_back(make_int4(kv.first.first, kv.first.second, kv.second[0],
-                                           kv.second.size() == 2 ? kv.second[1] : -1));
+            std::stable_sort(he.begin(), he.end(), [](const std::pair<uint64_t, int> &x, const std::pair<uint64_t, int> &y) {
+                return x.first < y.first;
+            });
+            for (size_t i = 0; i < he.size();) {
+                size_t j = i + 1;
+                while (j < he.size() && he[j].first == he[i].first) ++j;
+                if (j - i > 2) return fail("non-manifold mesh: an edge is shared by more than 2 faces");
+                if (j - i == 2 && he[i].second == he[i + 1].second) return fail("duplicated faces");
+                tp.adj.push_back(make_int4((int)(he[i].first >> 32), (int)(he[i].first & 0xffffffffu), he[i].second,
+                                           j - i == 2 ? he[i + 1].second : -1));
+                i = j;
             }
             tp.adj_off.push_back((int)tp.adj.size());
         }

@@ -226,6 +226,8 @@ _SIGNATURES = {
     "dtrt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dtrt_trace_closest": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int, c_int_p, c_float_p]),
     "dtrt_vol_read": (ctypes.c_int, [ctypes.c_char_p, c_int_p, c_int_p, c_float_p, c_float_p, c_float_p]),
+    "dtrt_rng_sequence": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_uint32), c_float_p, ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None

@@ -1404,6 +1404,18 @@ __global__ void __launch_bounds__(kBlock) k_trace(DevScene sc, const float *rays
     hits[2 * i + 1] = prim >= 0 ? sc.tris[prim].w : -1;
     t[i] = prim >= 0 ? th : INFINITY;
 }
+
+// Three fresh streams of RndSampler(seed, idx): raw outputs, FP32 and FP64 uniforms.
+__global__ void k_rng_sequence(uint64_t seed, uint64_t idx, int n, uint32_t *u32, float *f32, double *f64) {
+    const int which = threadIdx.x;  // one thread per stream: the draws are sequential
+    Rng r;
+    r.init(seed, idx);
+    for (int i = 0; i < n; ++i) {
+        if (which == 0) u32[i] = r.next_u32();
+        else if (which == 1) f32[i] = r.next1();
+        else f64[i] = r.next1d();
+    }
+}
 }  // namespace dt
 
 extern "C" {
@@ -1433,6 +1445,40 @@ int dtrt_trace_closest(dtrt_scene *scene, const float *rays, int n, int *hits, f
     cudaFree(dt_);
     if (e != cudaSuccess) {
         dt::set_last_error(std::string("dtrt_trace_closest: ") + cudaGetErrorString(e));
+        return DTRT_ERR_CUDA;
+    }
+    return DTRT_OK;
+}
+
+int dtrt_rng_sequence(uint64_t seed, uint64_t idx, int n, uint32_t *u32, float *f32, double *f64) {
+    if (n < 0 || n > (1 << 20)) {
+        dt::set_last_error("dtrt_rng_sequence: n must be in [0, 1<<20]");
+        return DTRT_ERR_INVALID;
+    }
+    if (n == 0) return DTRT_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        dt::set_last_error("no CUDA device");
+        return DTRT_ERR_NO_DEVICE;
+    }
+    void *buf = nullptr;
+    const size_t nb = (size_t)n * (4 + 4 + 8);
+    cudaError_t e = cudaMalloc(&buf, nb);
+    uint32_t *du = (uint32_t *)buf;
+    float *df = (float *)(du + n);
+    double *dd = (double *)((char *)buf + (size_t)n * 8);
+    if (e == cudaSuccess) {
+        dt::k_rng_sequence<<<1, 3>>>(seed, idx, n, du, df, dd);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && u32) e = cudaMemcpy(u32, du, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && f32) e = cudaMemcpy(f32, df, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && f64) e = cudaMemcpy(f64, dd, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(buf);
+    if (e != cudaSuccess) {
+        dt::set_last_error(std::string("dtrt_rng_sequence: ") + cudaGetErrorString(e));
         return DTRT_ERR_CUDA;
     }
     return DTRT_OK;

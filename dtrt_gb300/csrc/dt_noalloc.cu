@@ -12,7 +12,9 @@
 // caches it; make that first call before any stream capture. Every call shares the array
 // and leaves the previous call's contents behind; the render zeroes what must start at
 // zero (accumulators, queue counters, error flags). Calls that overlap on the GPU race on
-// the array and must be serialised by the caller.
+// the array and must be serialised by the caller. The cached address belongs to the
+// device's primary context: it is not looked up again after a device reset, and a
+// caller that renders under a context of its own creation is not supported.
 #include <mutex>
 
 #include "dt_host.h"
@@ -63,6 +65,12 @@ extern "C" int dtrt_render_fwd_noalloc(dtrt_scene *scene, const dtrt_render_opti
     }
     if (opts->spp < 0 || opts->sppse < 0) {
         dt::set_last_error("spp and sppse must be >= 0");
+        return DTRT_ERR_INVALID;
+    }
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != scene->device) {
+        cudaGetLastError();
+        dt::set_last_error("dtrt_render_fwd_noalloc: the current device is not the scene's device");
         return DTRT_ERR_INVALID;
     }
     unsigned char *scratch = nullptr;

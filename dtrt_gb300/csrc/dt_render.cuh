@@ -280,9 +280,23 @@ namespace dt {
 // fixed small queue capacities, no cudaMalloc / cudaFree / event creation.
 constexpr uint64_t kNoallocLiCap = 16384, kNoallocRecCap = 4096;
 
+constexpr size_t noalloc_round(size_t b) { return (b + 255) & ~(size_t)255; }
+// Bytes the carve below takes at its largest: DTRT_NOALLOC_MAX_PIXELS pixels with a host
+// output (staging copy) and the three queues at their fixed capacities.
+template <int N>
+constexpr size_t noalloc_worst_case_bytes() {
+    return noalloc_round((size_t)(N + 1) * DTRT_NOALLOC_MAX_PIXELS * 3 * 8) +
+           noalloc_round((size_t)N * DTRT_NOALLOC_MAX_PIXELS * 3 * 8) +
+           noalloc_round((size_t)(N + 1) * DTRT_NOALLOC_MAX_PIXELS * 3 * 4) + noalloc_round(32 * 8) +
+           noalloc_round(sizeof(unsigned int)) + noalloc_round(kNoallocLiCap * sizeof(LiTask<N>)) +
+           noalloc_round(kNoallocRecCap * sizeof(EdgeRec<N>)) + noalloc_round(kNoallocRecCap * sizeof(LinsRec<N>));
+}
+
 template <int N>
 int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t st,
                      unsigned char *scratch, size_t scratch_bytes) {
+    static_assert(noalloc_worst_case_bytes<N>() <= DTRT_NOALLOC_SCRATCH_BYTES,
+                  "the no-allocation scratch array cannot hold the largest allowed render");
     using clk = std::chrono::steady_clock;
     const auto t_start = clk::now();
     DevScene sc = s->dev;
@@ -426,6 +440,7 @@ int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, in
     ls.batches = batches;
     ls.kernel_launches = launches;
     ls.edge_samples = tot_edge * (uint64_t)rp.sppse;
+    ls.camera_schedule = DTRT_CAMERA_MEGAKERNEL;
     ls.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
     if (herr & ERR_QUEUE) {
         set_last_error("work queue overflow");

@@ -232,6 +232,43 @@ class Heterogeneous(Medium):
         self.d_albedo = _read(d_albedo, 3 * nder) if self.albedo_file is None else None
 
 
+def scene_spec(camera, shapes, bsdfs, emitters, phases, media):
+    """The scene description (dtrt_gb300.scenes.SceneSpec) of the dtrt objects a Scene
+    is constructed from: what the C ABI's dtrt_scene_create consumes."""
+    from . import scenes as S
+    cam = S.CameraSpec(camera.width, camera.height, camera.cam_to_world.reshape(4, 4),
+                       camera.cam_to_ndc.reshape(3, 3), camera.clip_near, camera.med_id,
+                       camera.velocities.reshape(-1, 3) if camera.velocities is not None else None, camera.rect)
+    spec = S.SceneSpec(camera._nder, cam, [], [])
+    for s in shapes:
+        spec.shapes.append(S.ShapeSpec(s.vertices, s.indices, s.bsdf_id, s.light_id, s.med_int_id, s.med_ext_id,
+                                       s.normals, s.uvs, s.velocities))
+    for b in bsdfs:
+        spec.bsdfs.append(S.BsdfSpec(b.type, diffuse=tuple(getattr(b, "diffuse", (0, 0, 0))),
+                                     specular=tuple(getattr(b, "specular", (0, 0, 0))),
+                                     exponent=getattr(b, "exponent", 0.0), alpha=getattr(b, "alpha", 0.1),
+                                     int_ior=getattr(b, "int_ior", 1.5), ext_ior=getattr(b, "ext_ior", 1.0),
+                                     d_diffuse=getattr(b, "d_diffuse", None),
+                                     d_specular=getattr(b, "d_specular", None),
+                                     d_exponent=getattr(b, "d_exponent", None),
+                                     d_alpha=getattr(b, "d_alpha", None), d_eta=getattr(b, "d_eta", None)))
+    for e in emitters:
+        spec.emitters.append(S.EmitterSpec(e.shape_id, tuple(e.intensity), e.type, e.two_sided, e.kappa,
+                                           e.d_intensity, e.d_kappa))
+    for p in phases:
+        spec.phases.append(S.PhaseSpec(p.type, p.g, p.d_g))
+    for m in media:
+        if m.type == _abi.MEDIUM_HOMOGENEOUS:
+            spec.media.append(S.MediumSpec(m.type, m.phase_id, m.sigma_t, tuple(m.albedo), m.d_sigma_t, m.d_albedo))
+        else:
+            spec.media.append(S.MediumSpec(m.type, m.phase_id, albedo=tuple(m.albedo), d_albedo=m.d_albedo,
+                                           density_file=m.density_file, albedo_file=m.albedo_file,
+                                           to_world=m.to_world.reshape(4, 4), density_scale=m.scale,
+                                           d_density_scale=m.d_scale, trans_velocities=m.trans_velocities,
+                                           rot_velocities=m.rot_velocities))
+    return spec
+
+
 class Scene:
     """Scene(camera, shapes, bsdfs, emitters, phases, media) (scene.cpp:9-136): the
     device scene (BVH, light and edge distributions) is built here."""
@@ -256,38 +293,7 @@ class Scene:
         return st
 
     def _spec(self, camera, shapes, bsdfs, emitters, phases, media):
-        from . import scenes as S
-        cam = S.CameraSpec(camera.width, camera.height, camera.cam_to_world.reshape(4, 4),
-                           camera.cam_to_ndc.reshape(3, 3), camera.clip_near, camera.med_id,
-                           camera.velocities.reshape(-1, 3) if camera.velocities is not None else None, camera.rect)
-        spec = S.SceneSpec(self._nder, cam, [], [])
-        for s in shapes:
-            spec.shapes.append(S.ShapeSpec(s.vertices, s.indices, s.bsdf_id, s.light_id, s.med_int_id, s.med_ext_id,
-                                           s.normals, s.uvs, s.velocities))
-        for b in bsdfs:
-            spec.bsdfs.append(S.BsdfSpec(b.type, diffuse=tuple(getattr(b, "diffuse", (0, 0, 0))),
-                                         specular=tuple(getattr(b, "specular", (0, 0, 0))),
-                                         exponent=getattr(b, "exponent", 0.0), alpha=getattr(b, "alpha", 0.1),
-                                         int_ior=getattr(b, "int_ior", 1.5), ext_ior=getattr(b, "ext_ior", 1.0),
-                                         d_diffuse=getattr(b, "d_diffuse", None),
-                                         d_specular=getattr(b, "d_specular", None),
-                                         d_exponent=getattr(b, "d_exponent", None),
-                                         d_alpha=getattr(b, "d_alpha", None), d_eta=getattr(b, "d_eta", None)))
-        for e in emitters:
-            spec.emitters.append(S.EmitterSpec(e.shape_id, tuple(e.intensity), e.type, e.two_sided, e.kappa,
-                                               e.d_intensity, e.d_kappa))
-        for p in phases:
-            spec.phases.append(S.PhaseSpec(p.type, p.g, p.d_g))
-        for m in media:
-            if m.type == _abi.MEDIUM_HOMOGENEOUS:
-                spec.media.append(S.MediumSpec(m.type, m.phase_id, m.sigma_t, tuple(m.albedo), m.d_sigma_t, m.d_albedo))
-            else:
-                spec.media.append(S.MediumSpec(m.type, m.phase_id, albedo=tuple(m.albedo), d_albedo=m.d_albedo,
-                                               density_file=m.density_file, albedo_file=m.albedo_file,
-                                               to_world=m.to_world.reshape(4, 4), density_scale=m.scale,
-                                               d_density_scale=m.d_scale, trans_velocities=m.trans_velocities,
-                                               rot_velocities=m.rot_velocities))
-        return spec
+        return scene_spec(camera, shapes, bsdfs, emitters, phases, media)
 
     def initEdges(self, weights):
         """Secondary-edge sampling weight per shape (scene.h:37-39)."""

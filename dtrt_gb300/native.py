@@ -242,3 +242,15 @@ class Batch:
 
 def device_count():
     return _abi.load().dtrt_device_count()
+
+
+def rng_sequence(seed, idx, n):
+    """n draws of the device PCG32 stream RndSampler(seed, idx) (dtrt_rng_sequence):
+    raw uint32 outputs, FP32 uniforms and FP64 uniforms, each from a fresh stream."""
+    lib = _abi.load()
+    u = np.zeros(n, np.uint32)
+    f = np.zeros(n, np.float32)
+    d = np.zeros(n, np.float64)
+    _abi.check(lib.dtrt_rng_sequence(int(seed), int(idx), int(n), u.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                     f.ctypes.data_as(_abi.c_float_p), d.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return u, f, d

@@ -81,10 +81,10 @@ def _f(x):
     return float(x.reshape(-1)[0]) if torch.is_tensor(x) else float(x)
 
 
-def build_native_scene(*args, reuse=None):
-    """Native objects and the device scene from a flat argument list
-    (scene_renderer.py:110-316). Returns (scene, (H, W)). With `reuse` (a dtrt.Scene),
-    that scene is updated in place when its triangles match, else a new one is built."""
+def _native_objects(*args):
+    """The dtrt objects of a flat argument list (scene_renderer.py:110-316): camera,
+    shapes, bsdfs, lights, phases, media, the edge weights (or None), the output (H, W)
+    and the tensors that must stay alive while the objects are in use."""
     num_shapes, num_bsdfs, num_lights, num_medium, num_phases = args[0:5]
     cam_to_world, cam_to_ndc, clip_near, resolution, cam_med_id, cam_vel, rect = args[5:12]
     assert cam_to_world.is_contiguous()
@@ -183,6 +183,29 @@ def build_native_scene(*args, reuse=None):
             i += 3
         else:
             raise ValueError(f"unknown phase type {args[i]!r}")
+    weights = args[i].contiguous().float() if args[i] is not None else None
+    if rect[2] == -1 or rect[3] == -1:
+        hw = (resolution[1], resolution[0])
+    else:
+        hw = (rect[3], rect[2])
+    return (camera, shapes, bsdfs, lights, phases, media), weights, hw, keep
+
+
+def scene_spec(*args):
+    """The scene description (dtrt_gb300.scenes.SceneSpec) of a flat argument list, built
+    by the same parsing as render_scene but without a device (e.g. for a CPU check)."""
+    objs, weights, hw, keep = _native_objects(*args)
+    spec = dtrt.scene_spec(*objs)
+    if weights is not None:
+        spec.edge_weights = weights.numpy().copy()
+    return spec
+
+
+def build_native_scene(*args, reuse=None):
+    """Native objects and the device scene from a flat argument list
+    (scene_renderer.py:110-316). Returns (scene, (H, W)). With `reuse` (a dtrt.Scene),
+    that scene is updated in place when its triangles match, else a new one is built."""
+    (camera, shapes, bsdfs, lights, phases, media), weights, hw, keep = _native_objects(*args)
     scene = None
     if reuse is not None and reuse._nder == camera._nder:
         try:
@@ -193,13 +216,8 @@ def build_native_scene(*args, reuse=None):
                 raise
     if scene is None:
         scene = dtrt.Scene(camera, shapes, bsdfs, lights, phases, media)
-    if args[i] is not None:
-        w = args[i].contiguous().float()
-        scene.initEdges(dtrt.float_ptr(w.data_ptr()))
-    if rect[2] == -1 or rect[3] == -1:
-        hw = (resolution[1], resolution[0])
-    else:
-        hw = (rect[3], rect[2])
+    if weights is not None:
+        scene.initEdges(dtrt.float_ptr(weights.data_ptr()))
     return scene, hw
 
 

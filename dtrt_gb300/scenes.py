@@ -518,6 +518,18 @@ def config3(width=512, height=512, res=128, seed=3, nder=8, amp_jitter=None, par
     return SceneSpec(nder, _camera(width, height, nder=nder), shapes, bsdfs, emitters, phases, media, name="C3")
 
 
+def with_crop(spec, width, height, x=None, y=None):
+    """Render only a width x height window of the camera's image (dtrt Camera.set_rect,
+    src/dtrt.cpp:35-37); the window is centred when x / y are None."""
+    W, H = spec.camera.width, spec.camera.height
+    x = (W - width) // 2 if x is None else int(x)
+    y = (H - height) // 2 if y is None else int(y)
+    if not (0 <= x and 0 <= y and x + width <= W and y + height <= H):
+        raise ValueError("crop window outside the image")
+    spec.camera.crop = (x, y, int(width), int(height))
+    return spec
+
+
 def config4(index, seed=4, nder=1, side_scale=1.0, spp_scale=1.0):
     """One of the 64 uneven C4 scenes: an icosphere or a displaced plane of
     1k-50k triangles (log-uniform), 50% with a 32^3-128^3 blob grid. Image side

@@ -277,7 +277,12 @@ int dtrt_render_fwd(dtrt_scene *scene, const dtrt_render_options *opts, float *o
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress),
  * so make that first call before any stream capture. All calls share the one array:
  * calls whose work overlaps on the GPU (other streams, other host threads) race and
- * must be serialised by the caller. The call blocks until `out` is written. */
+ * must be serialised by the caller. The call blocks until `out` is written. The scene's
+ * device must be the current device (else DTRT_ERR_INVALID); the cached array address
+ * belongs to that device's primary context and is not looked up again after a device
+ * reset. The scene settings dtrt_scene_enable_counters, dtrt_scene_set_camera_schedule
+ * and dtrt_scene_set_queue_capacity do not apply here: this render always runs the
+ * megakernel schedule with fixed queue capacities and no work counters. */
 #define DTRT_NOALLOC_MAX_PIXELS 4096
 #define DTRT_NOALLOC_SCRATCH_BYTES (6u << 20)
 int dtrt_render_fwd_noalloc(dtrt_scene *scene, const dtrt_render_options *opts, float *out,
@@ -425,6 +430,12 @@ int dtrt_batch_destroy(dtrt_batch *batch);
  * traversal. rays: [n][8] = org.xyz, tmin, dir.xyz, tmax (host arrays).
  * hits: [n][2] int = (global triangle id or -1, shape id); t: [n] float. */
 int dtrt_trace_closest(dtrt_scene *scene, const float *rays, int n, int *hits, float *t);
+
+/* Draws of the device PCG32 stream RndSampler(seed, idx) (src/sampler.cpp:3-41), for
+ * bit-exact tests of the generator every device kernel uses: u32[n] raw outputs,
+ * f32[n] the FP32 uniforms and f64[n] the FP64 uniforms, each from a fresh stream of
+ * the same (seed, idx). Any output pointer may be NULL. Host arrays; n <= 1<<20. */
+int dtrt_rng_sequence(uint64_t seed, uint64_t idx, int n, uint32_t *u32, float *f32, double *f64);
 
 /* Mitsuba VOL v3 grid reader (gridvolume.h:88-132). Pass data == NULL to query
  * res/channels/bounds; then call again with data of res_x*res_y*res_z*channels floats. */

@@ -52,7 +52,7 @@ def test_c0_homogeneous_sphere_parity(native, oracle):
     spec = scenes.config0(32, 32)
     kw = dict(spp=16, max_bounces=5, sppe=0, sppse=10)
     g = gpu_runs(native, spec, range(100, 116), **kw)
-    c = cpu_runs(oracle, spec, range(200, 208), **kw)
+    c = cpu_runs(oracle, spec, range(200, 216), **kw)
     print(assert_parity(g, c, label="C0"))
 
 
@@ -60,7 +60,7 @@ def test_c0_primary_edge_parity(native, oracle):
     spec = scenes.config0(32, 32)
     with native.NativeScene(spec) as s:
         g = np.stack([s.render(seed=sd, spp=0, max_bounces=5, sppe=64, sppse=0)[1:].copy() for sd in range(16)])
-    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=64, max_bounces=5) for sd in range(8)])
+    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=64, max_bounces=5) for sd in range(100, 116)])
     print(assert_parity(g, c, label="C0 primary"))
 
 
@@ -68,15 +68,15 @@ def test_c1_heterogeneous_parity(native, oracle):
     spec = scenes.config1(32, 32, res=32)
     kw = dict(spp=16, max_bounces=6, sppe=0, sppse=10)
     g = gpu_runs(native, spec, range(300, 316), **kw)
-    c = cpu_runs(oracle, spec, range(400, 408), **kw)
+    c = cpu_runs(oracle, spec, range(400, 416), **kw)
     print(assert_parity(g, c, label="C1"))
 
 
 def test_c2_mesh_derivative_parity(native, oracle):
     spec = scenes.config2(32, 32, subdiv=3, nder=4)
     kw = dict(spp=8, max_bounces=3, sppe=0, sppse=4)
-    g = gpu_runs(native, spec, range(500, 516), **kw)
-    c = cpu_runs(oracle, spec, range(600, 608), **kw)
+    g = gpu_runs(native, spec, range(500, 564), **kw)  # edge terms: heavy tails, more runs
+    c = cpu_runs(oracle, spec, range(600, 632), **kw)
     print(assert_parity(g, c, label="C2"))
 
 
@@ -98,7 +98,7 @@ def test_primary_edge_parity_moving_diffuse_sphere(native, oracle):
             if sd == 0:  # same projected-edge table: same sample count ceil(PDFsum*sppe/128)*128
                 assert s.last_stats()["primary_edge_samples"] == int(np.ceil(psum * sppe / 128.0)) * 128
         g = np.stack(g)
-    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=sppe, max_bounces=3) for sd in range(48)])
+    c = np.stack([oracle.render_primary_edges(spec, seed=sd, sppe=sppe, max_bounces=3) for sd in range(100, 148)])
     assert np.abs(c).sum() > 0 and np.abs(g).sum() > 0
     print(assert_parity(g, c, label="primary edges (moving sphere)"))
 
@@ -107,5 +107,5 @@ def test_full_forward_render_moving_diffuse_sphere(native, oracle):
     spec = _translating_diffuse_sphere(32, 32)
     kw = dict(spp=16, max_bounces=3, sppe=64, sppse=4)
     g = gpu_runs(native, spec, range(700, 716), **kw)
-    c = cpu_runs(oracle, spec, range(800, 808), **kw)
+    c = cpu_runs(oracle, spec, range(800, 816), **kw)
     print(assert_parity(g, c, label="moving sphere all terms"))

@@ -60,3 +60,23 @@ def test_noalloc_device_output_and_size_limit(native):
         st, _ = _render(lib, s.handle, big, "dtrt_render_fwd_noalloc", seed=0, spp=1, max_bounces=1, sppe=0, sppse=0)
         assert st == 1
         assert b"maximum is 4096" in lib.dtrt_last_error()
+
+
+def test_noalloc_largest_layout_and_limits(native):
+    """The largest layout the array must hold (8 derivative slots, 64x64 = 4096 pixels,
+    host output with its staging copy), and the option limits it rejects."""
+    lib = _abi.load()
+    spec = scenes.config2(64, 64, subdiv=3, nder=8)
+    kw = dict(spp=4, max_bounces=3, sppe=16, sppse=4)
+    with native.NativeScene(spec) as s:
+        st, ref = _render(lib, s.handle, spec, "dtrt_render_fwd", seed=3, **kw)
+        assert st == 0, lib.dtrt_last_error()
+        for call in range(2):
+            st, got = _render(lib, s.handle, spec, "dtrt_render_fwd_noalloc", seed=3, **kw)
+            assert st == 0, lib.dtrt_last_error()
+            np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6, err_msg=f"call {call}")
+        assert s.last_stats()["camera_schedule"] == _abi.CAMERA_MEGAKERNEL
+        for bad in (dict(kw, max_bounces=32), dict(kw, sppse=8193)):
+            st, _ = _render(lib, s.handle, spec, "dtrt_render_fwd_noalloc", seed=3, **bad)
+            assert st == 1
+            assert b"max_bounces <= 31 and sppse <= 8192" in lib.dtrt_last_error()

@@ -219,11 +219,13 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     stage = {"ms_camera": 0.0, "ms_edge": 0.0, "ms_li": 0.0, "ms_primary": 0.0}
     launches = 0
+    runs = []  # the timed renders' images, kept (after the step's end event) for the FP64 comparison
     for k in range(args.steps):
         flush.zero_()  # L2 flushed between timed steps (not timed)
         ev[k][0].record(stream)
         scene.render(out.data_ptr(), stream=sptr, **render_kw(wl_name, k))
         ev[k][1].record(stream)
+        runs.append(out.clone())
         st = scene.last_stats()
         for key in stage:
             stage[key] += st[key]
@@ -250,8 +252,12 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     dom = max(kms, key=kms.get)
     ki = kernels.index(dom)
     node_b, tri_b, grid_b = 64, 48, 32
-    alg_bytes = (node_b * cstats["k_node_visits"][ki] + tri_b * cstats["k_tri_tests"][ki] +
-                 grid_b * cstats["k_grid_lookups"][ki])
+    probe_b = 8 * light_cdf_probes(spec)  # one FP32/FP64 CDF entry per binary-search step
+    state_b = cstats["camera_state_bytes"] if dom == "camera" else 0
+    alg_terms = {"bvh_nodes": node_b * cstats["k_node_visits"][ki], "triangles": tri_b * cstats["k_tri_tests"][ki],
+                 "grid_lookups": grid_b * cstats["k_grid_lookups"][ki],
+                 "light_cdf_probes": probe_b * cstats["k_light_samples"][ki], "path_state": state_b}
+    alg_bytes = sum(alg_terms.values())
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -271,9 +277,11 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": kname,
                 "peak_source": "measured" if peaks else "fallback",
-                "bytes_per_step": alg_bytes,
-                "bytes_model": "64 B per BVH node visit + 48 B per triangle test + 32 B per trilinear lookup "
-                               "(device counters of one instrumented render)",
+                "bytes_per_step": alg_bytes, "bytes_per_step_terms": alg_terms,
+                "bytes_model": "64 B per BVH node visit + 48 B per triangle test + 32 B per trilinear lookup + "
+                               "8 B per light-CDF probe (binary-search steps per emitter sample) + the wavefront "
+                               "path-state bytes read and written per vertex launch (CamState + VertexIn; device "
+                               "counters of one instrumented render)",
                 "traffic_note": "dram read+write per step scaled from one ncu-captured launch (profiles/traffic.json)"}
     line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -290,9 +298,16 @@ def run_gpu(args, wl_name, rank, world, local_rank):
                                   "tri_tests": cstats["tri_tests"] / paths_per_step,
                                   "grid_lookups": cstats["grid_lookups"] / paths_per_step,
                                   "edge_records": cstats["edge_records"] / paths_per_step,
-                                  "li_tasks": cstats["li_tasks"] / paths_per_step}}
+                                  "li_tasks": cstats["li_tasks"] / paths_per_step,
+                                  "light_samples": cstats["light_samples"] / paths_per_step,
+                                  "camera_state_bytes": cstats["camera_state_bytes"] / paths_per_step}}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(wl_name, args.cpu_seconds_per_step, args.size)
+        line["cpu_baseline"], cpu_imgs = cpu_baseline(wl_name, args.cpu_seconds_per_step, args.size, keep_images=True)
+        line["error_vs_fp64"] = error_vs_fp64(torch.stack(runs).cpu().numpy(), cpu_imgs, wl["spp"],
+                                              line["cpu_baseline"]["spp_per_run"])
+    runs.clear()
+    if rank == 0 and not args.no_c3:
+        line["c3_forward"] = c3_forward(args.no_cpu_baseline)
     if rank == 0 and not args.no_grad_rmse:
         line["adjoint"] = adjoint_throughput_c3()
         line["grad_rmse"] = grad_rmse_c3(size=args.grad_size)
@@ -649,18 +664,96 @@ def scene_update_c2(iters=6, step=0.002, seed=5):
             "update_phases_ms": {k: med([s[k] for s in stats]) for k in ("ms_bvh", "ms_arrays", "ms_device")}}
 
 
-def cpu_baseline(wl_name, target_s, size=None):
+def cpu_baseline(wl_name, target_s, size=None, keep_images=False, runs=8):
+    """The oracle port on all host cores over a bounded sample of the workload: the full
+    image, `runs` independent renders of equal spp taking about target_s seconds in all."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
     wl = WORKLOADS[wl_name]
     spec = build_spec(wl_name, size)
     cores = os.cpu_count() or 1
     spp, _ = choose_cpu_spp(oracle_py, spec, wl_name, target_s=target_s, nthreads=cores)
+    per_run = max(1, spp // runs)
+    imgs = []
     t0 = time.perf_counter()
-    oracle_py.render(spec, **dict(render_kw(wl_name, 7), spp=spp), nthreads=cores)
+    for r in range(runs):
+        imgs.append(oracle_py.render(spec, **dict(render_kw(wl_name, 7 + r), spp=per_run), nthreads=cores))
     dt = time.perf_counter() - t0
-    return {"value": spec.width * spec.height * spp / dt, "unit": "paths/s", "cores": cores, "kind": "port",
-            "sample": f"full {spec.width}x{spec.height} image at {spp} spp ({dt:.1f} s)", "cpu": cpu_model()}
+    res = {"value": spec.width * spec.height * per_run * runs / dt, "unit": "paths/s", "cores": cores, "kind": "port",
+           "sample": f"full {spec.width}x{spec.height} image, {runs} renders at {per_run} spp ({dt:.1f} s)",
+           "spp_per_run": per_run, "cpu": cpu_model()}
+    return (res, np.stack(imgs)) if keep_images else res
+
+
+def error_vs_fp64(gpu_runs, cpu_runs, gpu_spp, cpu_spp, block=16):
+    """Error of the timed GPU renders (FP32 paths, FP64 accumulation) against the FP64
+    oracle's renders of the same workload (the CPU baseline's). Per slot (image, then each
+    derivative image): the relative error of the whole-image mean with its standard error
+    from the run-to-run spread, and the block z-test (block x block pixels): the fraction
+    of blocks beyond 3 sigma next to the fraction a correct renderer gives by chance
+    (Student t with the Welch degrees of freedom)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import statcheck
+    out = {"gpu_renders": int(gpu_runs.shape[0]), "gpu_spp_per_render": gpu_spp,
+           "oracle_renders": int(cpu_runs.shape[0]), "oracle_spp_per_render": cpu_spp, "block_pixels": block,
+           "slots": []}
+    z, ma, mb, se, df = statcheck.zscores(gpu_runs, cpu_runs, block)
+    for sl in range(gpu_runs.shape[1]):
+        g = gpu_runs[:, sl].astype(np.float64).mean(axis=(1, 2, 3))
+        c = cpu_runs[:, sl].astype(np.float64).mean(axis=(1, 2, 3))
+        ref = abs(c.mean()) if abs(c.mean()) > 0 else 1.0
+        sem = float(np.sqrt(g.var(ddof=1) / len(g) + c.var(ddof=1) / len(c)) / ref)
+        live = se[sl] > 0
+        zs = z[sl][live]
+        out["slots"].append({"slot": sl, "mean_rel_error": float(abs(g.mean() - c.mean()) / ref),
+                             "mean_rel_error_se": sem, "blocks": int(zs.size),
+                             "frac_blocks_beyond_3sigma": float((np.abs(zs) > 3).mean()) if zs.size else 0.0,
+                             "null_frac": statcheck.null_exceedance_prob(df[sl][live]) if zs.size else 0.0})
+    return out
+
+
+def light_cdf_probes(spec):
+    """Binary-search steps of one emitter sample: the light CDF, then the light shape's
+    triangle-area CDF (scene.cpp:45-98, upper_bound over each)."""
+    nl = max(1, len(spec.emitters))
+    nt = max([spec.shapes[e.shape_id].indices.shape[0] for e in spec.emitters] or [1])
+    return int(math.ceil(math.log2(nl + 1)) + math.ceil(math.log2(nt + 1)))
+
+
+def c3_forward(no_cpu=False, steps=3, warmup=1, cpu_target_s=4.0):
+    """Forward mode on the largest single-GPU configuration, C3 (512x512, 128 spp, depth 16,
+    nder 8: density scale, albedo, g, grid translation x/y/z, rotation about y and x; 128^3
+    grid), device-resident output, CUDA events; and the oracle port on the host cores over
+    a bounded sample (the full image at a reduced spp)."""
+    import torch
+    from dtrt_gb300 import native
+    spec = build_spec("c3")
+    kw = lambda seed: render_kw("c3", seed)
+    stream = torch.cuda.current_stream()
+    out = torch.empty(spec.out_shape(), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    paths = spec.width * spec.height * WORKLOADS["c3"]["spp"]
+    with native.NativeScene(spec) as sc:
+        for k in range(warmup):
+            sc.render(out.data_ptr(), stream=stream.cuda_stream, **kw(600 + k))
+        ms = []
+        for k in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sc.render(out.data_ptr(), stream=stream.cuda_stream, **kw(k))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    res = {"workload": WORKLOADS["c3"]["desc"], "width": 512, "height": 512, "spp": WORKLOADS["c3"]["spp"],
+           "max_bounces": 16, "nder": 8, "paths_per_s": paths / (t / 1e3), "ms_per_render": t,
+           "derivative_samples_per_s": paths * 8 / (t / 1e3)}
+    if not no_cpu:
+        cb = cpu_baseline("c3", cpu_target_s, runs=1)
+        res["cpu_baseline"] = cb
+        res["speedup_vs_cpu"] = res["paths_per_s"] / cb["value"]
+    return res
 
 
 def main():
@@ -678,6 +771,7 @@ def main():
     ap.add_argument("--adjoint-only", action="store_true", help="time only the C3 density adjoint replay")
     ap.add_argument("--no-batch", action="store_true", help="skip the C4 batch leg")
     ap.add_argument("--no-update", action="store_true", help="skip the C2 scene rebuild leg")
+    ap.add_argument("--no-c3", action="store_true", help="skip the C3 forward-mode leg")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -124,6 +124,8 @@ class RenderStats(ctypes.Structure):
         ("ms_total", ctypes.c_double), ("ms_camera", ctypes.c_double), ("ms_edge", ctypes.c_double),
         ("ms_li", ctypes.c_double), ("ms_primary", ctypes.c_double), ("ms_setup", ctypes.c_double),
         ("counters_enabled", ctypes.c_int), ("camera_schedule", ctypes.c_int),
+        ("light_samples", ctypes.c_uint64), ("k_light_samples", ctypes.c_uint64 * 5),
+        ("camera_state_bytes", ctypes.c_uint64),
     ]
 
     def as_dict(self):
@@ -132,6 +134,18 @@ class RenderStats(ctypes.Structure):
             v = getattr(self, name)
             d[name] = list(v) if isinstance(v, ctypes.Array) else v
         return d
+
+
+BVH_AUTO, BVH_HOST, BVH_DEVICE = 0, 1, 2
+BVH_DEVICE_MIN_TRIS = 16384
+
+
+class BvhInfo(ctypes.Structure):
+    _fields_ = [("builder", ctypes.c_int), ("refit", ctypes.c_int), ("num_nodes", ctypes.c_int),
+                ("max_depth", ctypes.c_int), ("ms_build", ctypes.c_double)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 BATCH_MAX_ITEMS, BATCH_MAX_TRIALS = 256, 16
@@ -226,6 +240,8 @@ _SIGNATURES = {
     "dtrt_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "dtrt_trace_closest": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int, c_int_p, c_float_p]),
     "dtrt_vol_read": (ctypes.c_int, [ctypes.c_char_p, c_int_p, c_int_p, c_float_p, c_float_p, c_float_p]),
+    "dtrt_set_bvh_builder": (ctypes.c_int, [ctypes.c_int]),
+    "dtrt_scene_bvh_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BvhInfo)]),
     "dtrt_rng_sequence": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_uint32), c_float_p, ctypes.POINTER(ctypes.c_double)]),
 }

@@ -14,7 +14,7 @@ LIB = os.path.join(OUT, "libdtrt_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
            "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
-UNITS = ["dt_api.cu", "dt_noalloc.cu", "dt_adjoint.cu", "dt_batch.cu", "dt_primal.cu", "dt_vadjoint.cu", "dt_render_n1.cu", "dt_render_n3.cu", "dt_render_n4.cu", "dt_render_n8.cu", "dt_bvh.cpp"]
+UNITS = ["dt_api.cu", "dt_noalloc.cu", "dt_adjoint.cu", "dt_batch.cu", "dt_primal.cu", "dt_vadjoint.cu", "dt_render_n1.cu", "dt_render_n3.cu", "dt_render_n4.cu", "dt_render_n8.cu", "dt_bvh.cpp", "dt_bvh_build.cu"]
 
 
 def _nvcc():

@@ -134,10 +134,10 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     std::memset(sc.cam.d_cpos, 0, sizeof(sc.cam.d_cpos));
     std::memset(sc.cam.d_cframe, 0, sizeof(sc.cam.d_cframe));
     if (!sb.err) DT_ACK(cudaMalloc(&sb.err, sizeof(unsigned int)));
-    if (!sb.counts) DT_ACK(cudaMalloc(&sb.counts, 32 * sizeof(unsigned long long)));
+    if (!sb.counts) DT_ACK(cudaMalloc(&sb.counts, kCountSlots * sizeof(unsigned long long)));
     sc.error_flags = sb.err;
     DT_ACK(cudaMemsetAsync(sb.err, 0, sizeof(unsigned int), st));
-    DT_ACK(cudaMemsetAsync(sb.counts, 0, 32 * sizeof(unsigned long long), st));
+    DT_ACK(cudaMemsetAsync(sb.counts, 0, kCountSlots * sizeof(unsigned long long), st));
     unsigned long long *ctr = s->counters ? sb.counts + 8 : nullptr;
     // ---------------------------------------------------------------- inputs and outputs
     const float *dimg = nullptr;
@@ -237,6 +237,7 @@ int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_i
     ls.k_node_visits[0] = ls.node_visits = hc[1];
     ls.k_tri_tests[0] = ls.tri_tests = hc[2];
     ls.k_grid_lookups[0] = ls.grid_lookups = hc[3];
+    ls.k_light_samples[0] = ls.light_samples = hc[4];
     ls.ms_camera = ms_replay;
     ls.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
     if (herr & ERR_STACK) {

@@ -7,6 +7,7 @@
 // headers), Scene light tables (src/scene.cpp:45-98), the secondary-edge manager
 // (src/edge_manager/bruteforce.cpp:4-20) and primary-edge projection
 // (src/edge_manager/edge_manager.cpp:6-110, include/line_clip.h:37-95).
+#include <atomic>
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -198,6 +199,16 @@ struct Builder {
             return false;
         }
         return true;
+    }
+    // take over a device allocation written elsewhere (never reused from the old scene, so
+    // a failed update leaves the old scene's arrays untouched)
+    template <class T>
+    void adopt(T *p, size_t bytes, const T **dst) {
+        s->allocs.push_back(p);
+        s->alloc_bytes.push_back(bytes);
+        taken.push_back(0);
+        *dst = p;
+        ++allocated;
     }
     // deferred copies (reuse mode)
     int commit() {
@@ -585,8 +596,37 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
         // a new tree halves the cost.
         constexpr double kRefitCostLimit = 2.0;
         const auto tb = std::chrono::steady_clock::now();
-        bool refit = cached && !rebuild_bvh && !tp.bvh.nodes.empty();
+        const int choice = bvh_builder_setting();
+        bool on_device = choice == DTRT_BVH_DEVICE || (choice == DTRT_BVH_AUTO && ttot >= DTRT_BVH_DEVICE_MIN_TRIS);
+        if (on_device && ttot >= 2) {
+            DeviceBvh db;
+            std::string err;
+            const int r = build_bvh_device(tv, ttot, db, err);
+            if (r == 2) {
+                set_last_error(err);
+                return DTRT_ERR_CUDA;
+            }
+            on_device = r == 0;
+            if (on_device) {
+                tp.bvh = BvhBuildOut();  // updates build this tree again instead of refitting a host copy
+                tp.sah_build = 0.0;
+                ds.num_nodes = db.num_nodes;
+                bld.adopt(db.nodes, (size_t)db.num_nodes * sizeof(BvhNode), &ds.nodes);
+                bld.adopt(db.leaf_tris, db.leaf_tris_bytes, &ds.leaf_tris);
+                const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
+                s->bvh_info = dtrt_bvh_info{DTRT_BVH_DEVICE, 0, db.num_nodes, db.max_depth, ms};
+                if (info) {
+                    info->bvh_refit = 0;
+                    info->sah_ratio = 1.f;
+                    info->ms_bvh = ms;
+                }
+            }
+        } else {
+            on_device = false;
+        }
+        bool refit = !on_device && cached && !rebuild_bvh && !tp.bvh.nodes.empty();
         double ratio = 1.0;
+        if (!on_device) {
         if (refit) {
             refit_bvh(tv, tp.bvh);
             ratio = tp.sah_build > 0.0 ? bvh_sah_cost(tp.bvh) / tp.sah_build : 1.0;
@@ -603,6 +643,9 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
         }
         ds.num_nodes = (int)tp.bvh.nodes.size();
         if (!bld.upload(tp.bvh.nodes, &ds.nodes) || !bld.upload(tp.bvh.leaf_tris, &ds.leaf_tris)) return DTRT_ERR_CUDA;
+        s->bvh_info = dtrt_bvh_info{DTRT_BVH_HOST, refit ? 1 : 0, ds.num_nodes, tp.bvh.max_depth,
+                                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count()};
+        }
     }
     // ------------------------------------------------------------ materials
     std::vector<DevBsdf> bsdfs(d->num_bsdfs);
@@ -1083,10 +1126,31 @@ int check_grid_medium(const dtrt_scene *s, int medium_id) {
 }
 
 }  // namespace
+std::atomic<int> g_bvh_builder{DTRT_BVH_AUTO};
+int bvh_builder_setting() { return g_bvh_builder.load(); }
+
 }  // namespace dt
 
 // ====================================================================== C ABI
 extern "C" {
+
+int dtrt_set_bvh_builder(int builder) {
+    if (builder != DTRT_BVH_AUTO && builder != DTRT_BVH_HOST && builder != DTRT_BVH_DEVICE) {
+        dt::set_last_error("unknown BVH builder");
+        return DTRT_ERR_INVALID;
+    }
+    dt::g_bvh_builder.store(builder);
+    return DTRT_OK;
+}
+
+int dtrt_scene_bvh_info(const dtrt_scene *scene, dtrt_bvh_info *out) {
+    if (!scene || !out) {
+        dt::set_last_error("null argument");
+        return DTRT_ERR_INVALID;
+    }
+    *out = scene->bvh_info;
+    return DTRT_OK;
+}
 
 int dtrt_abi_version(void) { return DTRT_ABI_VERSION; }
 
@@ -1221,6 +1285,7 @@ int dtrt_scene_update(dtrt_scene *scene, const dtrt_scene_desc *desc, unsigned f
     scene->density_voxels = t->density_voxels;
     scene->num_shapes = t->num_shapes;
     scene->topo = std::move(t->topo);
+    scene->bvh_info = t->bvh_info;
     st = dt::set_edge_weights(scene, desc->edge_weights);
     if (st == DTRT_OK && dgrid) st = dt::upload_media(scene);
     info.buffers_reused = bld.reused;

@@ -2,6 +2,7 @@
 // Replaces the Embree scene build of the reference (src/scene.cpp:17-43).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include "dt_scene.h"
@@ -28,5 +29,21 @@ void refit_bvh(const std::vector<float> &tri_verts, BvhBuildOut &tree);
 // area(node) plus, over leaves, triangles x area(leaf), all divided by area(root). A refit
 // tree whose cost grows well past its cost at build time traverses slowly and is rebuilt.
 double bvh_sah_cost(const BvhBuildOut &tree);
+
+// A tree built on the device (dt_bvh_build.cu): device allocations owned by the caller.
+struct DeviceBvh {
+    BvhNode *nodes = nullptr;
+    float4 *leaf_tris = nullptr;
+    int num_nodes = 0;
+    size_t leaf_tris_bytes = 0;
+    int max_depth = 0;  // of the uncollapsed binary tree (bounds the traversal stack)
+};
+
+// Linear BVH of the triangles on the current device, in the layout build_bvh writes
+// (2-wide nodes, leaves of <= 4 triangles, (v0, id) (e1) (e2) records in leaf order).
+// Returns 0 on success; 1 for fewer than two triangles; 2 on a CUDA error (message in
+// err); 3 when the tree is deeper than the traversal stack allows (nothing allocated:
+// build on the host instead).
+int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBvh &out, std::string &err);
 
 }  // namespace dt

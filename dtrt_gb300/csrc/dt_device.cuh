@@ -11,7 +11,7 @@ namespace dt {
 
 // Per-thread work counters, flushed once per thread when counters are enabled.
 struct Ctr {
-    uint32_t rays = 0, nodes = 0, tris = 0, lookups = 0;
+    uint32_t rays = 0, nodes = 0, tris = 0, lookups = 0, lights = 0;  // lights: emitter samples (CDF searches)
 };
 
 DT_D void set_error(const DevScene &sc, unsigned int bit) {
@@ -1243,6 +1243,7 @@ DT_HEAVY float3 nee_point(const DevScene &sc, int *stack, float3 p, const float 
                       float3 &wo, float &pdf, Ctr &c) {
     float3 lp, ln;
     const int l = sample_light(sc, rnd, lp, ln, pdf);
+    ++c.lights;
     if (l < 0) return mk(0.f, 0.f, 0.f);
     float3 dir = lp - p;
     if (dot(dir, ln) < 0.f && pdf != 0.f) {
@@ -1263,6 +1264,7 @@ DT_HEAVY float3 nee_surface(const DevScene &sc, int *stack, const Its &its, cons
                         int max_inter, float3 &wo, float &pdf, bool flag, Ctr &c) {
     float3 lp, ln;
     const int l = sample_light(sc, rnd, lp, ln, pdf);
+    ++c.lights;
     if (l < 0) return mk(0.f, 0.f, 0.f);
     float3 dir = lp - its.p;
     const bool transmissive = sc.bsdfs[sc.shapes[sc.emitters[l].shape_id].bsdf_id].type == BSDF_NULL ||
@@ -1292,6 +1294,7 @@ DT_HEAVY DV<N> nee_point_ad(const DevScene &sc, int *stack, const DV<N> &p, cons
     float3 lp, ln;
     float pdf0;
     const int l = sample_light(sc, rnd, lp, ln, pdf0);
+    ++c.lights;
     if (l < 0) return DV<N>();
     float3 dir = lp - p.val();
     if (dot(dir, ln) < 0.f) {
@@ -1318,6 +1321,7 @@ DT_HEAVY DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &it
     float3 lp, ln;
     float pdf0;
     const int l = sample_light(sc, rnd, lp, ln, pdf0);
+    ++c.lights;
     if (l < 0) return DV<N>();
     float3 dir = lp - its.p.val();
     const int lb = sc.bsdfs[sc.shapes[sc.emitters[l].shape_id].bsdf_id].type;

@@ -41,9 +41,12 @@ struct SceneTopology {
     std::vector<int4> adj;                   // per shape: (a, b, f0, f1 or -1), shape-local, sorted by (a, b)
     std::vector<int> adj_off;                // num_shapes + 1 offsets into adj
     std::vector<int> media_type, media_res;  // per medium: type; density resolution (3 ints)
-    BvhBuildOut bvh;                         // the tree as last built or refit
+    BvhBuildOut bvh;                         // the tree as last built or refit (host builds)
     double sah_build = 0.0;                  // its surface-area cost right after the last full build
 };
+
+// Process-wide choice of the BVH builder for scenes created or updated afterwards.
+int bvh_builder_setting();
 
 }  // namespace dt
 
@@ -65,6 +68,7 @@ struct dtrt_scene {
     std::vector<void *> dgrid_bufs;         // per medium: per-voxel derivative directions (owned)
     long long density_voxels = 0;           // voxels of all heterogeneous media (adjoint gradient length)
     dt::SceneTopology topo;
+    dtrt_bvh_info bvh_info{};               // how the current tree was made
 };
 
 namespace dt {

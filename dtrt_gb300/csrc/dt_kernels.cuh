@@ -68,19 +68,23 @@ struct Queue {
     unsigned long long cap;
 };
 
-// Counter slots: [kernel][rays, nodes, tris, lookups] then three task counts
+// Counter slots: [kernel][rays, nodes, tris, lookups, light samples] then three task counts
 enum { K_CAMERA = 0, K_EDGE, K_LI, K_LINS, K_PRIMARY };
-enum { CT_EDGE_SAMPLES = 20, CT_LI, CT_PRIMARY, CT_NUM };
+constexpr int kCtrPerKernel = 5;
+enum { CT_EDGE_SAMPLES = 5 * kCtrPerKernel, CT_LI, CT_PRIMARY, CT_NUM };
+// device counter buffer: 8 queue / scratch counts, then the CT_NUM work counters
+constexpr int kCountSlots = 64;
+static_assert(8 + CT_NUM <= kCountSlots, "counter slots");
 
 DT_D void flush_counters(unsigned long long *ctr, int kernel, const Ctr &c, uint32_t extra_slot = 0xffffffffu,
                          uint32_t extra = 0) {
     if (!ctr) return;
-    unsigned long long v[4] = {c.rays, c.nodes, c.tris, c.lookups};
+    unsigned long long v[kCtrPerKernel] = {c.rays, c.nodes, c.tris, c.lookups, c.lights};
     const unsigned mask = __activemask();
     bool lead = true;
     if (mask == 0xffffffffu) {  // full warp: reduce with shuffles, one atomic per counter
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kCtrPerKernel; ++k) {
             unsigned long long x = v[k];
             for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(mask, x, off);
             v[k] = x;
@@ -88,8 +92,8 @@ DT_D void flush_counters(unsigned long long *ctr, int kernel, const Ctr &c, uint
         lead = (threadIdx.x & 31) == 0;
     }
     if (lead)
-        for (int k = 0; k < 4; ++k)
-            if (v[k]) atomicAdd(ctr + 4 * kernel + k, v[k]);
+        for (int k = 0; k < kCtrPerKernel; ++k)
+            if (v[k]) atomicAdd(ctr + kCtrPerKernel * kernel + k, v[k]);
     if (extra_slot != 0xffffffffu && extra) atomicAdd(ctr + extra_slot, (unsigned long long)extra);
 }
 

@@ -148,10 +148,10 @@ int render_primal(dtrt_scene *s, const dtrt_render_options *o, float *out, int o
     rp.npix = rp.out_w * rp.out_h;
     const size_t npix = (size_t)rp.npix;
     if (!sb.err) DT_PCK(cudaMalloc(&sb.err, sizeof(unsigned int)));
-    if (!sb.counts) DT_PCK(cudaMalloc(&sb.counts, 32 * sizeof(unsigned long long)));
+    if (!sb.counts) DT_PCK(cudaMalloc(&sb.counts, kCountSlots * sizeof(unsigned long long)));
     sc.error_flags = sb.err;
     DT_PCK(cudaMemsetAsync(sb.err, 0, sizeof(unsigned int), st));
-    DT_PCK(cudaMemsetAsync(sb.counts, 0, 32 * sizeof(unsigned long long), st));
+    DT_PCK(cudaMemsetAsync(sb.counts, 0, kCountSlots * sizeof(unsigned long long), st));
     unsigned long long *ctr = s->counters ? sb.counts + 8 : nullptr;
     if (!ensure_buffer((void **)&sb.adj_img, &sb.adj_img_n, npix * 3 * 8)) return DTRT_ERR_CUDA;
     DT_PCK(cudaMemsetAsync(sb.adj_img, 0, npix * 3 * 8, st));
@@ -242,6 +242,7 @@ int render_primal(dtrt_scene *s, const dtrt_render_options *o, float *out, int o
     ls.k_node_visits[0] = ls.node_visits = hc[1];
     ls.k_tri_tests[0] = ls.tri_tests = hc[2];
     ls.k_grid_lookups[0] = ls.grid_lookups = hc[3];
+    ls.k_light_samples[0] = ls.light_samples = hc[4];
     ls.ms_camera = ms;
     ls.ms_total = std::chrono::duration<double, std::milli>(clk::now() - t_start).count();
     if (herr & ERR_STACK) {

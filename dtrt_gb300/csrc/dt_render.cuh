@@ -67,12 +67,12 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         !ensure_buffer(&sb.qe, &sb.qe_bytes, rec_cap * sizeof(EdgeRec<N>)) ||
         !ensure_buffer(&sb.ql, &sb.ql_bytes, rec_cap * sizeof(LinsRec<N>)))
         return DTRT_ERR_CUDA;
-    if (!sb.counts) DT_CK(cudaMalloc(&sb.counts, 32 * sizeof(unsigned long long)));
+    if (!sb.counts) DT_CK(cudaMalloc(&sb.counts, kCountSlots * sizeof(unsigned long long)));
     if (!sb.err) DT_CK(cudaMalloc(&sb.err, sizeof(unsigned int)));
     sc.error_flags = sb.err;
     DT_CK(cudaMemsetAsync(sb.acc1, 0, acc1_n * 8, st));
     DT_CK(cudaMemsetAsync(sb.acc2, 0, acc2_n * 8, st));
-    DT_CK(cudaMemsetAsync(sb.counts, 0, 32 * sizeof(unsigned long long), st));
+    DT_CK(cudaMemsetAsync(sb.counts, 0, kCountSlots * sizeof(unsigned long long), st));
     DT_CK(cudaMemsetAsync(sb.err, 0, sizeof(unsigned int), st));
     unsigned long long *ctr = s->counters ? sb.counts + 8 : nullptr;
     Queue qe{sb.qe, sb.counts + 0, rec_cap}, ql{sb.ql, sb.counts + 1, rec_cap}, qli{sb.qli, sb.counts + 2, li_cap};
@@ -106,6 +106,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     };
     auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
     uint64_t tot_edge = 0, tot_lins = 0, tot_li = 0, batches = 0;
+    uint64_t state_traffic = 0;  // wavefront path-state bytes read + written (counted when counters are on)
     bool used_wavefront = false;
     int rc = DTRT_OK;
     // Li tasks are drained chunk by chunk so that the queue never exceeds li_cap
@@ -175,6 +176,19 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                      })))
                     return rc;
                 launches += 2 * levels + 1;  // start, 2 per level (1 at level 0), accumulation
+                if (ctr) {
+                    // every launched vertex reads and writes its path's state and vertex inputs;
+                    // the start writes them once per path, the accumulation reads the sums
+                    std::vector<unsigned long long> lc((size_t)2 * (levels + 1));
+                    DT_CK(cudaMemcpyAsync(lc.data(), vcnt, lc.size() * sizeof(unsigned long long),
+                                          cudaMemcpyDeviceToHost, st));
+                    DT_CK(cudaStreamSynchronize(st));
+                    const uint64_t sv = sizeof(CamState<N>) + sizeof(VertexIn<N>);
+                    uint64_t launched = 0;
+                    for (int L = 0; L < levels; ++L) launched += lc[L] + (L > 0 ? lc[levels + 1 + L] : 0);
+                    state_traffic += 2 * sv * launched + sv * (uint64_t)rp.path_count +
+                                   sizeof(DV<N>) * (uint64_t)rp.path_count;
+                }
             } else if ((rc = timed(ms_camera, [&] {
                             k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);
                         }))) {
@@ -241,15 +255,19 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     ls.counters_enabled = ctr != nullptr;
     ls.camera_schedule = used_wavefront ? DTRT_CAMERA_WAVEFRONT : DTRT_CAMERA_MEGAKERNEL;
     for (int k = 0; k < 5; ++k) {
-        ls.k_rays[k] = hc[4 * k];
-        ls.k_node_visits[k] = hc[4 * k + 1];
-        ls.k_tri_tests[k] = hc[4 * k + 2];
-        ls.k_grid_lookups[k] = hc[4 * k + 3];
-        ls.rays += hc[4 * k];
-        ls.node_visits += hc[4 * k + 1];
-        ls.tri_tests += hc[4 * k + 2];
-        ls.grid_lookups += hc[4 * k + 3];
+        const unsigned long long *h = hc + kCtrPerKernel * k;
+        ls.k_rays[k] = h[0];
+        ls.k_node_visits[k] = h[1];
+        ls.k_tri_tests[k] = h[2];
+        ls.k_grid_lookups[k] = h[3];
+        ls.k_light_samples[k] = h[4];
+        ls.rays += h[0];
+        ls.node_visits += h[1];
+        ls.tri_tests += h[2];
+        ls.grid_lookups += h[3];
+        ls.light_samples += h[4];
     }
+    ls.camera_state_bytes = state_traffic;
     ls.edge_samples = ctr ? hc[CT_EDGE_SAMPLES] : tot_edge * (uint64_t)rp.sppse;
     ls.ms_camera = ms_camera;
     ls.ms_edge = ms_edge;

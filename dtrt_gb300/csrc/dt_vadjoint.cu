@@ -86,10 +86,10 @@ int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const flo
     std::memset(sc.cam.d_cpos, 0, sizeof(sc.cam.d_cpos));
     std::memset(sc.cam.d_cframe, 0, sizeof(sc.cam.d_cframe));
     if (!sb.err) DT_VCK(cudaMalloc(&sb.err, sizeof(unsigned int)));
-    if (!sb.counts) DT_VCK(cudaMalloc(&sb.counts, 32 * sizeof(unsigned long long)));
+    if (!sb.counts) DT_VCK(cudaMalloc(&sb.counts, kCountSlots * sizeof(unsigned long long)));
     sc.error_flags = sb.err;
     DT_VCK(cudaMemsetAsync(sb.err, 0, sizeof(unsigned int), st));
-    DT_VCK(cudaMemsetAsync(sb.counts, 0, 32 * sizeof(unsigned long long), st));
+    DT_VCK(cudaMemsetAsync(sb.counts, 0, kCountSlots * sizeof(unsigned long long), st));
     unsigned long long *ctr = s->counters ? sb.counts + 8 : nullptr;
     // ---------------------------------------------------------------- buffers
     const float *dimg = d_image;

@@ -279,6 +279,17 @@ class Scene:
         from .native import NativeScene
         self.native = NativeScene(self.spec)
 
+    @classmethod
+    def from_spec(cls, spec):
+        """A Scene built directly from a dtrt_gb300.scenes.SceneSpec (same device scene as
+        the constructor would build from the equivalent dtrt objects)."""
+        from .native import NativeScene
+        self = cls.__new__(cls)
+        self._nder = spec.nder
+        self.spec = spec
+        self.native = NativeScene(spec)
+        return self
+
     def update(self, camera, shapes, bsdfs, emitters, phases, media, rebuild_bvh=False):
         """Rebuild this scene in place from objects with the same triangles (same shapes,
         vertex and triangle counts, index lists; same media types and grid sizes): the BVH
@@ -380,9 +391,23 @@ class VolPathTracerSimple(Integrator):
 
 
 def _require_surface_scene(scene, name):
-    if scene.spec.media:
+    """The reference's surface integrators trace no media, test light visibility with one
+    occlusion query (scene.cpp:150-175, 302-392: a null-BSDF surface blocks light) and
+    sample lights only in front of the shading normal (scene.cpp:316), so lights behind a
+    transmissive surface are reached by BSDF sampling alone while still MIS-weighted
+    against light sampling. The volumetric estimator has the same expectation only
+    without media, null BSDFs and transmissive BSDFs; other scenes are refused."""
+    spec = scene.spec
+    if spec.media or spec.camera.med_id >= 0:
         raise NotImplementedError(f"{name} ignores participating media in the reference; dtrt_gb300 renders it "
                                   "for surface scenes only (use VolPathTracerAD)")
+    for b in spec.bsdfs:
+        if b.type == _abi.BSDF_NULL:
+            raise NotImplementedError(f"{name}: a null-BSDF surface blocks light in the reference's visibility test "
+                                      "but is crossed by the volumetric estimator (use VolPathTracerAD)")
+        if b.type == _abi.BSDF_ROUGHDIELECTRIC:
+            raise NotImplementedError(f"{name}: the reference's light sampling skips lights behind a transmissive "
+                                      "surface, which changes its expectation (use VolPathTracerAD)")
 
 
 class PathTracerAD(VolPathTracerAD):

@@ -93,6 +93,12 @@ class NativeScene:
         _abi.check(self.lib.dtrt_scene_set_density_derivatives(self.handle, int(medium_id),
                                                                g.ctypes.data_as(_abi.c_float_p)))
 
+    def bvh_info(self):
+        """How the scene's BVH was made (dtrt_scene_bvh_info): builder, nodes, depth, time."""
+        bi = _abi.BvhInfo()
+        _abi.check(self.lib.dtrt_scene_bvh_info(self.handle, ctypes.byref(bi)))
+        return bi.as_dict()
+
     def last_stats(self):
         st = _abi.RenderStats()
         _abi.check(self.lib.dtrt_scene_last_stats(self.handle, ctypes.byref(st)))
@@ -254,3 +260,10 @@ def rng_sequence(seed, idx, n):
     _abi.check(lib.dtrt_rng_sequence(int(seed), int(idx), int(n), u.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
                                      f.ctypes.data_as(_abi.c_float_p), d.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
     return u, f, d
+
+
+def set_bvh_builder(builder):
+    """'auto', 'host' or 'device' (dtrt_set_bvh_builder): the BVH builder of scenes created
+    or updated afterwards, process-wide."""
+    v = {"auto": _abi.BVH_AUTO, "host": _abi.BVH_HOST, "device": _abi.BVH_DEVICE}
+    _abi.check(_abi.load().dtrt_set_bvh_builder(v[builder] if isinstance(builder, str) else int(builder)))

@@ -191,6 +191,9 @@ typedef struct {
     double ms_setup;          /* scene upload / derived data for this render        */
     int counters_enabled;
     int camera_schedule;      /* DTRT_CAMERA_MEGAKERNEL or DTRT_CAMERA_WAVEFRONT (forward renders) */
+    uint64_t light_samples;   /* emitter samples (light and area CDF searches)        */
+    uint64_t k_light_samples[5];
+    uint64_t camera_state_bytes; /* wavefront camera stage: path-state bytes read + written */
 } dtrt_render_stats;
 
 /* Opaque scene handle (device-resident geometry, BVH, media, edge tables). */
@@ -425,6 +428,31 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
 int dtrt_batch_launch(dtrt_batch *batch, void *stream);
 int dtrt_batch_stats_get(const dtrt_batch *batch, dtrt_batch_stats *out);
 int dtrt_batch_destroy(dtrt_batch *batch);
+
+/* ---------------------------------------------------------------- BVH builder
+ * Replaces the Embree scene build of the reference (src/scene.cpp:17-43), which runs on
+ * the host for every Scene. DTRT_BVH_HOST: binned-SAH build on the host (leaves of <= 8
+ * triangles; updates refit it). DTRT_BVH_DEVICE: linear BVH built on the GPU (Morton
+ * codes, radix sort, radix tree, bottom-up boxes; leaves of <= 4 triangles; updates build
+ * it again), falling back to the host build when the tree would be deeper than the
+ * traversal stack. DTRT_BVH_AUTO (default): the device build from
+ * DTRT_BVH_DEVICE_MIN_TRIS triangles. The setting is process-wide and applies to scenes
+ * created or updated afterwards. Closest hits do not depend on the tree except at exact
+ * ties. */
+#define DTRT_BVH_AUTO 0
+#define DTRT_BVH_HOST 1
+#define DTRT_BVH_DEVICE 2
+#define DTRT_BVH_DEVICE_MIN_TRIS 16384
+int dtrt_set_bvh_builder(int builder);
+
+typedef struct {
+    int builder;        /* DTRT_BVH_HOST or DTRT_BVH_DEVICE: the builder that made the tree */
+    int refit;          /* 1: the last update refit the host tree instead of building it */
+    int num_nodes;
+    int max_depth;      /* host: tree depth; device: depth of the binary tree before leaf collapse */
+    double ms_build;    /* wall time of the build or refit (device: kernels and copies included) */
+} dtrt_bvh_info;
+int dtrt_scene_bvh_info(const dtrt_scene *scene, dtrt_bvh_info *out);
 
 /* Closest-hit queries against the scene BVH (device kernel), for tests of the
  * traversal. rays: [n][8] = org.xyz, tmin, dir.xyz, tmax (host arrays).

@@ -37,6 +37,16 @@ int oracle_render(const dtrt_scene_desc *desc, const dtrt_render_options *opts, 
 int oracle_render_ext(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads,
                       unsigned est_flags, const float *const *density_dirs);
 
+/* oracle_render with another AD integrator behind IntegratorAD::render:
+ * ORACLE_VOLPATH_AD (VolPathTracerAD, volpathAD.cpp), ORACLE_PATH_AD (PathTracerAD,
+ * pathAD.cpp:10-228) or ORACLE_DIRECT_AD (DirectIntegratorAD, directAD.cpp:1-163).
+ * The last two accept surface scenes only (no media, no null BSDFs). */
+#define ORACLE_VOLPATH_AD 0
+#define ORACLE_PATH_AD 1
+#define ORACLE_DIRECT_AD 2
+int oracle_render_integrator(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads,
+                             int integrator);
+
 /* VolPathTracer::render (src/integrator/volpath.cpp:105-140): the primal image
  * out[H][W][3] (no derivatives), written unconditionally. */
 int oracle_render_primal(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads);

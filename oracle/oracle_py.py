@@ -35,6 +35,7 @@ def lib():
         L.oracle_render_primary_edges.argtypes = [SD, RO, fp, ctypes.c_int]
         L.oracle_render_ext.argtypes = [SD, RO, fp, ctypes.c_int, ctypes.c_uint, ctypes.POINTER(fp)]
         L.oracle_render_primal.argtypes = [SD, RO, fp, ctypes.c_int]
+        L.oracle_render_integrator.argtypes = [SD, RO, fp, ctypes.c_int, ctypes.c_int]
         L.oracle_pcg32.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]
         L.oracle_pcg32.restype = None
         L.oracle_next1d.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, dp]
@@ -64,6 +65,24 @@ def render(spec, seed=0, spp=4, max_bounces=5, sppe=0, sppse=10, mode=-1, ddist=
                             nthreads)
     if r:
         raise RuntimeError("oracle_render: " + lib().oracle_last_error().decode())
+    return out
+
+
+INTEGRATORS = {"volpath": 0, "path": 1, "direct": 2}
+
+
+def render_integrator(spec, integrator, seed=0, spp=4, max_bounces=5, sppe=0, sppse=10, mode=-1, ddist=0.0,
+                      nthreads=0):
+    """render() with the reference's other AD integrators: 'volpath' (VolPathTracerAD),
+    'path' (PathTracerAD) or 'direct' (DirectAD); the last two on surface scenes only."""
+    desc, keep = spec.to_desc()
+    out = np.zeros(spec.out_shape(), np.float32)
+    o = _opts(seed, spp, max_bounces, sppe, sppse, mode, ddist)
+    r = lib().oracle_render_integrator(ctypes.byref(desc), ctypes.byref(o),
+                                       out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), nthreads,
+                                       INTEGRATORS[integrator])
+    if r:
+        raise RuntimeError("oracle_render_integrator: " + lib().oracle_last_error().decode())
     return out
 
 

@@ -858,6 +858,321 @@ struct Integrator {
         return ret;
     }
 
+    // ================================================================ surface integrators
+    // PathTracerAD (pathAD.cpp:10-213) and DirectIntegratorAD (directAD.cpp:7-150): surface
+    // scenes only. Their own random-number order, MIS heuristics, occlusion test and edge
+    // parametrisations are restated; media are not traced (the reference ignores them).
+
+    // Scene::isVisible, scene.cpp:150-175
+    bool is_visible(const V3 &p, bool p_on_surface, const V3 &q, bool q_on_surface) const {
+        V3 dir = q - p;
+        double dist = norm(dir);
+        dir = dir / dist;
+        int s, pr;
+        double th;
+        return !sc.trace(p, dir, p_on_surface ? kShadowEps : 0.0, q_on_surface ? (1.0 - kShadowEps) * dist : dist, s,
+                         pr, th);
+    }
+
+    // Scene::pdfEmitterSample, scene.cpp:526-536, divided by the geometry term at the hit
+    double emitter_hit_pdf(int shape, double dist_sq, double cos_wi) const {
+        int l = sc.shapes[shape].light_id;
+        return sc.light_pmf[l] / sc.light_areas[l] / (cos_wi / dist_sq);
+    }
+
+    // AreaLight::eval / AreaLightEx::evalAD with an explicit normal (area.cpp:13-15, area2.cpp:13-27)
+    DV3<N> emitter_eval_ad(const Emitter<N> &e, const DV3<N> &n, const DV3<N> &w) const {
+        if (e.type == DTRT_EMITTER_AREA)
+            return (e.two_sided || dot(val(n), val(w)) > 0) ? lift<N>(e.intensity_val()) : DV3<N>();
+        Dual<N> t = dot(n, w);
+        if (t.v > kEps) return e.intensity * (d_exp(e.kappa * (t - 1.0)) * e.kappa * kInvTwoPi);
+        return DV3<N>();
+    }
+
+    // Scene::sampleEmitterDirect, scene.cpp:302-345: one occlusion test from the shading
+    // point (no null-interface pass-through); the segment counts only when the sampled
+    // light's own triangle closes it within ShadowEpsilon.
+    V3 sample_emitter_direct(const Its &its, const double rnd[4], V3 &wo, double &pdf) const {
+        V3 lp, ln;
+        int l = sc.sample_light(rnd, lp, ln, pdf);
+        V3 dir = lp - its.p;
+        if (dot(dir, its.sh.n) > 0 && dot(dir, ln) < 0 && pdf != 0) {
+            double dist = norm(dir);
+            dir = dir / dist;
+            int s, pr;
+            double th;
+            if (sc.trace(its.p, dir, kShadowEps, INFINITY, s, pr, th) && s == sc.emitters[l].shape_id) {
+                Its ni;
+                sc.shape_intersect(s, pr, Ray{its.p, dir}, ni);
+                if (std::abs(ni.t - dist) < kShadowEps) {
+                    pdf *= dist * dist / dot(ln, -dir);
+                    wo = its.to_local(dir);
+                    return le_normal(sc.emitters[l], ni.sh.n, -dir) / pdf;
+                }
+            }
+        }
+        return V3();
+    }
+
+    // Scene::sampleEmitterDirectAD, scene.cpp:347-392
+    DV3<N> sample_emitter_direct_ad(const ItsAD<N> &its, const double rnd[4], DV3<N> &wo, double &pdf) const {
+        V3 lp, ln;
+        int l = sc.sample_light(rnd, lp, ln, pdf);
+        V3 dir = lp - val(its.p);
+        if (dot(dir, val(its.sh.n)) > 0 && dot(dir, ln) < 0 && pdf != 0) {
+            double dist = norm(dir);
+            dir = dir / dist;
+            int s, pr;
+            double th;
+            if (sc.trace(val(its.p), dir, kShadowEps, INFINITY, s, pr, th) && s == sc.emitters[l].shape_id) {
+                ItsAD<N> ni;
+                sc.shape_intersect_ad(s, pr, RayAD<N>{its.p, lift<N>(dir)}, ni);
+                if (std::abs(ni.t.v - dist) < kShadowEps) {
+                    pdf *= dist * dist / dot(ln, -dir);
+                    wo = its.to_local(lift<N>(dir));
+                    return emitter_eval_ad(sc.emitters[l], ni.sh.n, lift<N>(-dir)) / pdf;
+                }
+            }
+        }
+        return DV3<N>();
+    }
+
+    // PathTracerAD::Li, pathAD.cpp:10-58 (the non-AD sub-path of its edge term and of the
+    // primary edges)
+    V3 path_li(Rng &rng, const Ray &ray_in, int max_depth) const {
+        Ray ray = ray_in;
+        Its its;
+        V3 ret;
+        sc.ray_intersect(ray, true, its);
+        if (!its.valid()) return ret;
+        V3 thr(1, 1, 1);
+        int depth = 0;
+        while (depth <= max_depth && its.valid()) {
+            const Shape<N> &sh = sc.shapes[its.shape];
+            if (sh.is_emitter() && depth == 0) ret += cmul(thr, sc.le(its, -ray.d));
+            if (depth >= max_depth) break;
+            double r4[4] = {rng.next1(), rng.next1(), rng.next1(), rng.next1()};
+            double pdf_nee;
+            V3 wo;
+            V3 value = sample_emitter_direct(its, r4, wo, pdf_nee);
+            if (!is_zero(value, 1e-12)) {
+                V3 bv = sc.bsdf_eval(its, wo);
+                double bp = sc.bsdf_pdf(its, wo);
+                ret += cmul(cmul(thr, value), bv) * mis(pdf_nee, bp);
+            }
+            double r3[3] = {rng.next1(), rng.next1(), rng.next1()};
+            double bpdf, beta;
+            V3 bw = sc.bsdf_sample(its, r3, wo, bpdf, beta);
+            if (is_zero(bw, 1e-12)) break;
+            wo = its.to_world(wo);
+            ray = Ray{its.p, wo};
+            if (!sc.ray_intersect(ray, true, its)) break;
+            thr = cmul(thr, bw);
+            if (sc.shapes[its.shape].is_emitter()) {
+                V3 lc = sc.le(its, -ray.d);
+                if (!is_zero(lc, 1e-12)) {
+                    double pn = emitter_hit_pdf(its.shape, sq_norm(its.p - ray.o), its.wi.z);
+                    ret += cmul(thr, lc) * mis(bpdf, pn);
+                }
+            }
+            depth++;
+        }
+        return ret;
+    }
+
+    // PathTracerAD::LiAD, pathAD.cpp:61-213 (ALTERNATIVE_EDGE_SAMPLING)
+    DV3<N> path_li_ad(const ItsAD<N> &its, Rng &rng, const RayAD<N> &ray_in, int max_depth, int mode,
+                      bool inc_emission) const {
+        if (mode == 0) return DV3<N>();
+        DV3<N> ret;
+        if (!its.valid()) return ret;
+        const Shape<N> &sh = sc.shapes[its.shape];
+        if (sh.is_emitter() && (mode & DTRT_MODE_EMISSION) && inc_emission) ret += sc.le_ad(its, -ray_in.d);
+        if (max_depth == 0) return ret;
+        Its its0 = its.plain();
+        DV3<N> wo;
+        double pdf_nee;
+        if (mode & DTRT_MODE_SURFACE_MAIN) {
+            double r4[4] = {rng.next1(), rng.next1(), rng.next1(), rng.next1()};
+            DV3<N> value = sample_emitter_direct_ad(its, r4, wo, pdf_nee);
+            if (!is_zero(value, kEps)) {
+                DV3<N> bv = sc.bsdf_eval_ad(its, wo);
+                double bp = sc.bsdf_pdf(its0, val(wo));
+                ret += cmul(value, bv) * mis(pdf_nee, bp);
+            }
+        }
+        double r3[3] = {rng.next1(), rng.next1(), rng.next1()};
+        double bpdf, beta;
+        DV3<N> value = sc.bsdf_sample_ad(its, r3, wo, bpdf, beta);
+        if (!is_zero(value, kEps)) {
+            wo = zero_grad(its.to_world(wo));  // asserted derivative-free at pathAD.cpp:97
+            RayAD<N> ray{its.p, wo};
+            ItsAD<N> its1;
+            if (sc.ray_intersect_ad(ray, true, its1)) {
+                if (sc.shapes[its1.shape].is_emitter() && (mode & DTRT_MODE_SURFACE_MAIN)) {
+                    DV3<N> lc = sc.le_ad(its1, -ray.d);
+                    if (!is_zero(val(lc), 1e-12)) {
+                        double pn = emitter_hit_pdf(its1.shape, sq_norm(val(its1.p) - val(ray.o)), its1.wi.z.v);
+                        ret += cmul(value, lc) * mis(bpdf, pn);
+                    }
+                }
+                ret += cmul(value, path_li_ad(its1, rng, ray, max_depth - 1, mode, false));
+            }
+        }
+        if (sppse > 0 && (mode & DTRT_MODE_SURFACE_BOUNDARY) && sc.edges_distrb.size() > 0) {
+            std::vector<V3> der(N);
+            V3 x1v = val(its.p);
+            for (int i = 0; i < sppse; ++i) {
+                double rnd = rng.next1();
+                int sid;
+                double epdf;
+                const Edge *e = sc.sample_edge(x1v, rnd, sid, epdf);
+                if (!e) continue;
+                double t = rnd;
+                const Shape<N> &shape = sc.shapes[sid];
+                if (!shape.is_silhouette(*e, x1v)) continue;
+                DV3<N> w1;
+                double dist;
+                V3 nrm;
+                if (!edge_direction(shape, *e, its.p, t, epdf, w1, dist, nrm)) continue;
+                if (der_is_zero(w1, kEps)) continue;
+                V3 bval = sc.bsdf_eval(its0, its0.to_local(val(w1)));
+                if (is_zero(bval, kEps)) continue;
+                if (!is_visible(x1v, true, x1v + val(w1) * dist, true)) continue;
+                V3 w2 = normalized(val(w1) - nrm * kAngleEps);
+                V3 delta = path_li(rng, Ray{x1v, w2}, max_depth - 1);
+                w2 = normalized(val(w1) + nrm * kAngleEps);
+                delta -= path_li(rng, Ray{x1v, w2}, max_depth - 1);
+                if (is_zero(delta, kEps)) continue;
+                for (int j = 0; j < N; ++j) der[j] += cmul(bval, delta) * (dot(nrm, grad(w1, j)) / epdf);
+            }
+            for (int j = 0; j < N; ++j) {
+                ret.x.d[j] += der[j].x / sppse;
+                ret.y.d[j] += der[j].y / sppse;
+                ret.z.d[j] += der[j].z / sppse;
+            }
+        }
+        return ret;
+    }
+
+    // DirectIntegratorAD::radiance, directAD.cpp:110-140 (power heuristic)
+    V3 direct(Rng &rng, const Ray &ray_in) const {
+        Ray ray = ray_in;
+        Its its;
+        V3 ret;
+        sc.ray_intersect(ray, true, its);
+        if (!its.valid()) return ret;
+        if (sc.shapes[its.shape].is_emitter()) ret += sc.le(its, -ray.d);
+        double r4[4] = {rng.next1(), rng.next1(), rng.next1(), rng.next1()};
+        double pdf_nee;
+        V3 wo;
+        V3 value = sample_emitter_direct(its, r4, wo, pdf_nee);
+        if (!is_zero(value, 1e-12)) {
+            V3 bv = sc.bsdf_eval(its, wo);
+            double bp = sc.bsdf_pdf(its, wo);
+            ret += cmul(value, bv) * mis(pdf_nee, bp);
+        }
+        double r3[3] = {rng.next1(), rng.next1(), rng.next1()};
+        double bpdf, beta;
+        V3 bw = sc.bsdf_sample(its, r3, wo, bpdf, beta);
+        if (!is_zero(bw, 1e-12)) {
+            wo = its.to_world(wo);
+            ray = Ray{its.p, wo};
+            if (sc.ray_intersect(ray, true, its) && sc.shapes[its.shape].is_emitter()) {
+                V3 lc = sc.le(its, -ray.d);
+                if (!is_zero(lc, 1e-12)) {
+                    double pn = emitter_hit_pdf(its.shape, sq_norm(its.p - ray.o), its.wi.z);
+                    ret += cmul(bw, lc) * mis(bpdf, pn);
+                }
+            }
+        }
+        return ret;
+    }
+
+    // DirectIntegratorAD::radianceAD, directAD.cpp:7-107: balance-heuristic MIS, and the
+    // edge term of the first hit with the linear edge parametrisation (sinTheta / dist
+    // Jacobian) and emitter-only delta functions
+    DV3<N> direct_ad(Rng &rng, const RayAD<N> &ray_in) const {
+        RayAD<N> ray = ray_in;
+        ItsAD<N> its;
+        DV3<N> ret;
+        sc.ray_intersect_ad(ray, true, its);
+        if (!its.valid()) return ret;
+        if (sc.shapes[its.shape].is_emitter()) ret += sc.le_ad(its, -ray.d);
+        Its its0 = its.plain();
+        {
+            double r4[4] = {rng.next1(), rng.next1(), rng.next1(), rng.next1()};
+            double pdf_nee;
+            DV3<N> wo;
+            DV3<N> value = sample_emitter_direct_ad(its, r4, wo, pdf_nee);
+            if (!is_zero(value, kEps)) {
+                DV3<N> bv = sc.bsdf_eval_ad(its, wo);
+                double bp = sc.bsdf_pdf(its0, val(wo));
+                ret += cmul(value, bv) * (pdf_nee / (pdf_nee + bp));
+            }
+            double r3[3] = {rng.next1(), rng.next1(), rng.next1()};
+            double bpdf, beta;
+            value = sc.bsdf_sample_ad(its, r3, wo, bpdf, beta);
+            if (!is_zero(value, kEps)) {
+                wo = zero_grad(its.to_world(wo));  // asserted derivative-free at directAD.cpp:38
+                RayAD<N> r1{its.p, wo};
+                ItsAD<N> its1;
+                if (sc.ray_intersect_ad(r1, true, its1) && sc.shapes[its1.shape].is_emitter()) {
+                    DV3<N> lc = sc.le_ad(its1, -r1.d);
+                    if (!is_zero(val(lc), 1e-12)) {
+                        double pn = emitter_hit_pdf(its1.shape, sq_norm(val(its1.p) - val(r1.o)), its1.wi.z.v);
+                        ret += cmul(value, lc) * (bpdf / (pn + bpdf));
+                    }
+                }
+            }
+        }
+        if (sppse > 0 && sc.edges_distrb.size() > 0) {
+            std::vector<V3> der(N);
+            const DV3<N> &x1 = its.p;
+            V3 x1v = val(x1);
+            for (int i = 0; i < sppse; ++i) {
+                // Scene::sampleEdge(p, frame, rnd, shape_id, t, pdf), scene.h:103-108
+                double t = rng.next1();
+                int sid;
+                double epdf;
+                const Edge *e = sc.sample_edge(x1v, t, sid, epdf);
+                if (!e) continue;
+                epdf /= e->length;
+                const Shape<N> &shape = sc.shapes[sid];
+                if (!shape.is_silhouette(*e, x1v)) continue;
+                const DV3<N> &v0 = shape.verts[e->v0], &v1 = shape.verts[e->v1];
+                DV3<N> y1 = v0 * (1.0 - t) + v1 * t, w1 = y1 - x1;
+                V3 tang = normalized(val(v1) - val(v0));
+                V3 nrm = normalized(cross(val(v0) - x1v, val(v1) - x1v));
+                Dual<N> dist = norm(w1);
+                w1 = w1 / dist;
+                double mx = 0;
+                for (int j = 0; j < N; ++j) mx = std::max(mx, std::abs(dot(grad(w1, j), val(w1))));
+                if (mx >= kEps) continue;  // asserted below Epsilon at directAD.cpp:75
+                V3 bval = sc.bsdf_eval(its0, its0.to_local(val(w1)));
+                if (is_zero(bval, kEps) || !is_visible(x1v, true, val(y1), true)) continue;
+                V3 delta;
+                Its its1;
+                V3 w2 = normalized(val(w1) - nrm * kAngleEps);
+                if (sc.ray_intersect(Ray{x1v, w2}, true, its1) && sc.shapes[its1.shape].is_emitter())
+                    delta += sc.le(its1, -val(w1));
+                w2 = normalized(val(w1) + nrm * kAngleEps);
+                if (sc.ray_intersect(Ray{x1v, w2}, true, its1) && sc.shapes[its1.shape].is_emitter())
+                    delta -= sc.le(its1, -val(w1));
+                if (is_zero(delta, kEps)) continue;
+                double cos_t = -dot(val(w1), tang), sin_t = std::sqrt(1.0 - cos_t * cos_t);
+                for (int j = 0; j < N; ++j)
+                    der[j] += cmul(bval, delta) * (dot(nrm, grad(w1, j)) * sin_t / (epdf * dist.v));
+            }
+            for (int j = 0; j < N; ++j) {
+                ret.x.d[j] += der[j].x / sppse;
+                ret.y.d[j] += der[j].y / sppse;
+                ret.z.d[j] += der[j].z / sppse;
+            }
+        }
+        return ret;
+    }
+
     // one Lins sample, volpathAD.cpp:337-441
     V3 lins_sample(const Its &its0, const V3 &n, const V3 &rd, int ph, int med, int max_depth, Rng &rng) const {
         V3 lins, wo, att;
@@ -960,13 +1275,25 @@ thread_local std::string g_err;
 
 template <int N>
 int render_impl(const dtrt_scene_desc &d, const dtrt_render_options &o, float *out, int nthreads, bool pass1,
-                bool pass2, unsigned est_flags = 0, const float *const *density_dirs = nullptr) {
+                bool pass2, unsigned est_flags = 0, const float *const *density_dirs = nullptr,
+                int integrator = ORACLE_VOLPATH_AD) {
     using namespace orc;
     auto sc = std::make_unique<Scene<N>>();
     std::string err = sc->build(d);
     if (!err.empty()) {
         g_err = err;
         return 1;
+    }
+    if (integrator != ORACLE_VOLPATH_AD) {  // the surface integrators trace no media
+        if (!sc->media.empty() || sc->cam.med_id >= 0) {
+            g_err = "PathTracerAD / DirectAD oracle: surface scenes only (no media)";
+            return 1;
+        }
+        for (const auto &b : sc->bsdfs)
+            if (b.is_null()) {
+                g_err = "PathTracerAD / DirectAD oracle: null BSDFs block light in the reference's occlusion test";
+                return 1;
+            }
     }
     sc->est_flags = est_flags;
     for (int mi = 0; density_dirs && mi < d.num_media; ++mi) {
@@ -1004,10 +1331,15 @@ int render_impl(const dtrt_scene_desc &d, const dtrt_render_options &o, float *o
                         jx = rng.next1();
                         jy = rng.next1();
                     }
-                    // pixelColorAD, volpathAD.cpp:632-642
+                    // pixelColorAD, volpathAD.cpp:632-642 / pathAD.cpp:222-228 / directAD.cpp:153-156
                     RayAD<N> ray = cam.sample_primary_ray_ad(ix + jx, iy + jy);
                     ItsAD<N> its;
-                    if (sc->ray_intersect_ad(ray, false, its)) acc += in.li_ad(its, rng, ray, cam.med_id, o.max_bounces, mode);
+                    if (integrator == ORACLE_DIRECT_AD) {
+                        acc += in.direct_ad(rng, ray);
+                    } else if (sc->ray_intersect_ad(ray, false, its)) {
+                        acc += integrator == ORACLE_PATH_AD ? in.path_li_ad(its, rng, ray, o.max_bounces, mode, true)
+                                                            : in.li_ad(its, rng, ray, cam.med_id, o.max_bounces, mode);
+                    }
                 }
                 acc = acc / (double)o.spp;
                 V3 v = val(acc);
@@ -1052,10 +1384,16 @@ int render_impl(const dtrt_scene_desc &d, const dtrt_render_options &o, float *o
                 if (!(tr > kEps)) continue;
                 const double delta = (double)1e-4f;
                 double x1 = px + p[0].v - nrm[0] * delta, y1 = py + p[1].v - nrm[1] * delta;
-                V3 dv = in.li(rng, cam.sample_primary_ray(x1, y1), o.max_bounces, cam.med_id);
+                // pixelColor of the integrator (volpathAD.cpp:622-629, pathAD.cpp:216-219, directAD.cpp:147-150)
+                auto pixel_color = [&](const Ray &r) {
+                    if (integrator == ORACLE_PATH_AD) return in.path_li(rng, r, o.max_bounces);
+                    if (integrator == ORACLE_DIRECT_AD) return in.direct(rng, r);
+                    return in.li(rng, r, o.max_bounces, cam.med_id);
+                };
+                V3 dv = pixel_color(cam.sample_primary_ray(x1, y1));
                 x1 = px + p[0].v + nrm[0] * delta;
                 y1 = py + p[1].v + nrm[1] * delta;
-                dv -= in.li(rng, cam.sample_primary_ray(x1, y1), o.max_bounces, cam.med_id);
+                dv -= pixel_color(cam.sample_primary_ray(x1, y1));
                 int lx = cropped ? px - cam.crop_x : px, ly = cropped ? py - cam.crop_y : py;
                 int lw = cropped ? cam.crop_w : cam.width, lh = cropped ? cam.crop_h : cam.height;
                 if (lx < 0 || ly < 0 || lx >= lw || ly >= lh) continue;  // edge point on the far image border
@@ -1138,6 +1476,15 @@ int oracle_render_ext(const dtrt_scene_desc *desc, const dtrt_render_options *op
     if (!desc || !opts || !out) { g_err = "null argument"; return 1; }
     return dispatch(desc->nder, [&](auto n) {
         return render_impl<decltype(n)::value>(*desc, *opts, out, nthreads, true, true, est_flags, density_dirs);
+    });
+}
+
+int oracle_render_integrator(const dtrt_scene_desc *desc, const dtrt_render_options *opts, float *out, int nthreads,
+                             int integrator) {
+    if (!desc || !opts || !out) { g_err = "null argument"; return 1; }
+    if (integrator < ORACLE_VOLPATH_AD || integrator > ORACLE_DIRECT_AD) { g_err = "unknown integrator"; return 1; }
+    return dispatch(desc->nder, [&](auto n) {
+        return render_impl<decltype(n)::value>(*desc, *opts, out, nthreads, true, true, 0, nullptr, integrator);
     });
 }
 

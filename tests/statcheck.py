@@ -7,10 +7,27 @@ with the Welch-Satterthwaite degrees of freedom, so a fraction p0 = P(|t| > 3) o
 blocks exceeds 3 by chance (0.27% for normal z, about 0.6% at 16 + 16 runs). The
 allowance for a slot with n blocks is the count that a Binomial(n, p0) exceeds with
 probability below `alpha` (1e-3 per slot): a correct renderer fails a slot about once
-in a thousand checks, a biased one in most."""
+in a thousand checks, a biased one in most.
+
+Edge-sampled derivative estimates are heavy-tailed: with few runs their sample variance is
+often too small and the t test too wide. The runs of each side are therefore grouped into
+`batches` batch means (consecutive runs averaged) before the test, so that each tested
+value is itself an average of many paths and close to normal; more runs per side then
+tighten the test instead of exposing the tails."""
 import numpy as np
 
 MIN_RUNS = 16
+BATCHES = 16
+
+
+def batch_means(x, batches=BATCHES):
+    """[K, ...] runs -> [batches, ...] means of consecutive groups (unchanged when K <= batches)."""
+    x = np.asarray(x)
+    K = x.shape[0]
+    if K <= batches:
+        return x
+    m = K // batches
+    return x[: m * batches].astype(np.float64).reshape((batches, m) + x.shape[1:]).mean(axis=1)
 
 
 def block_sums(imgs, b):
@@ -60,11 +77,14 @@ def null_exceedance_prob(df, z_max=3.0):
     return float(np.mean(2.0 * stats.t.sf(z_max, df))) if df.size else 0.0
 
 
-def assert_parity(a, b, block=4, z_max=3.0, alpha=1e-3, total_max=4.0, slots=None, label="", min_runs=MIN_RUNS):
+def assert_parity(a, b, block=4, z_max=3.0, alpha=1e-3, total_max=4.0, slots=None, label="", min_runs=MIN_RUNS,
+                  batches=BATCHES):
     """Fail when, in any slot, more non-empty blocks exceed z_max than the binomial allowance
     (null fraction from the t distribution, false-alarm rate alpha per slot), or when the
-    whole-image sum of a slot differs by more than total_max sigma."""
+    whole-image sum of a slot differs by more than total_max sigma. Each side's runs are
+    first reduced to `batches` batch means."""
     assert len(a) >= min_runs and len(b) >= min_runs, f"{label}: need >= {min_runs} runs per side"
+    a, b = batch_means(a, batches), batch_means(b, batches)
     z, ma, mb, se, df = zscores(a, b, block)
     tz, ta, tb, tse = total_z(a, b)
     S = z.shape[0]

@@ -19,8 +19,8 @@ from dtrt_gb300.scenes import BsdfSpec, EmitterSpec, MediumSpec, PhaseSpec, Scen
 pytestmark = pytest.mark.gpu
 
 RUNS = 16
-# more GPU than oracle runs: the edge-term estimates are heavy-tailed (see statcheck)
-GPU_RUNS, CPU_RUNS = 64, 32
+# runs per side, reduced to 16 batch means by statcheck (edge-term estimates are heavy-tailed)
+GPU_RUNS, CPU_RUNS = 256, 64
 
 
 def _pair(native, oracle, spec, kw, gruns=GPU_RUNS, cruns=CPU_RUNS):

@@ -143,3 +143,23 @@ def test_translation_derivative_matches_finite_difference(oracle):
     der, fd = np.array(der), np.array(fd)
     se = math.sqrt(der.var(ddof=1) / len(der) + fd.var(ddof=1) / len(fd))
     assert abs(der.mean() - fd.mean()) < 4 * se + 0.05 * abs(fd.mean()), (der, fd)
+
+
+@pytest.mark.parametrize("integrator,depth", [("path", 3), ("direct", 1)])
+def test_surface_integrators_share_the_volumetric_expectation(oracle, integrator, depth):
+    """The restated PathTracerAD / DirectAD (pathAD.cpp, directAD.cpp) and VolPathTracerAD
+    estimate the same image and derivative on an opaque surface scene: the relation the
+    GPU's mapping of those integrators onto the volumetric estimator rests on."""
+    import statcheck
+    spec = scenes.config2(24, 24, subdiv=3, nder=1)
+    nv = spec.shapes[0].vertices.shape[0]
+    spec.shapes[0].velocities = np.tile(np.array([[1.0, 0.0, 0.0]], np.float32), (nv, 1))
+    kw = dict(spp=16, max_bounces=depth, sppe=64, sppse=4)
+    a = np.stack([oracle.render_integrator(spec, integrator, seed=100 + k, **kw) for k in range(32)])
+    b = np.stack([oracle.render(spec, seed=900 + k, **kw) for k in range(32)])
+    print(statcheck.assert_parity(a, b, label=integrator))
+
+
+def test_surface_integrators_refuse_media(oracle):
+    with pytest.raises(RuntimeError, match="surface scenes only"):
+        oracle.render_integrator(scenes.config0(8, 8), "path", spp=1, max_bounces=2, sppse=0)

@@ -137,7 +137,7 @@ class RenderStats(ctypes.Structure):
 
 
 BVH_AUTO, BVH_HOST, BVH_DEVICE = 0, 1, 2
-BVH_DEVICE_MIN_TRIS = 16384
+BVH_DEVICE_MIN_TRIS = 65536
 
 
 class BvhInfo(ctypes.Structure):

@@ -935,17 +935,32 @@ DT_HEAVY void int_sig_t(const DevScene &sc, const DevMedium &m, const RayAD<N> &
         }
         return;
     }
-    for (int i = 0; i < 10; ++i) {
-        const float r = ((float)i + rng.next1()) * 0.1f;
-        const Df<N> tt = tmin + len * r;
-        const DV<N> pt = ray.o + ray.d * tt;
-        const Df<N> s = scale * grid_lookup_ad<N>(m.density, pt, c);
+    if (!m.density.moving && !(m.density.dgrid && m.density.dgrid_n == N) && ray.o.der_zero(0.f) &&
+        ray.d.der_zero(0.f) && tmin.der_zero(0.f) && !scatter) {
+        // sample positions without derivatives on a static grid: each sample's derivative is
+        // d_scale[j] * density(p), so the integral needs only the sum of ten plain lookups
+        const float3 o = ray.o.val(), d = ray.d.val();
+        float sum = 0.f;
 #pragma unroll
-        for (int j = 0; j < N; ++j) out[j] += s.d[j];
-        if (scatter) grid_scatter(m.density, adj->grad + m.grad_off, pt.val(), -adj->w * m.scale * len * 0.1f);
+        for (int i = 0; i < 10; ++i) {
+            const float r = ((float)i + rng.next1()) * 0.1f;
+            sum += grid_lookup(m.density, o + d * (tmin.v + len * r), c);
+        }
+#pragma unroll
+        for (int j = 0; j < N; ++j) out[j] = scale.d[j] * sum * (len * 0.1f);
+    } else {
+        for (int i = 0; i < 10; ++i) {
+            const float r = ((float)i + rng.next1()) * 0.1f;
+            const Df<N> tt = tmin + len * r;
+            const DV<N> pt = ray.o + ray.d * tt;
+            const Df<N> s = scale * grid_lookup_ad<N>(m.density, pt, c);
+#pragma unroll
+            for (int j = 0; j < N; ++j) out[j] += s.d[j];
+            if (scatter) grid_scatter(m.density, adj->grad + m.grad_off, pt.val(), -adj->w * m.scale * len * 0.1f);
+        }
+#pragma unroll
+        for (int j = 0; j < N; ++j) out[j] *= len * 0.1f;
     }
-#pragma unroll
-    for (int j = 0; j < N; ++j) out[j] *= len * 0.1f;
     const float3 o = ray.o.val(), d = ray.d.val();
     if (!tmax.der_zero(1e-6f)) {
         const float dv = m.scale * grid_lookup(m.density, o + d * (tmax.v - kEps), c);

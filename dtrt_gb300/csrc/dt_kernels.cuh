@@ -114,6 +114,24 @@ DT_D long long queue_reserve(const DevScene &sc, const Queue &q) {
     return (long long)slot;
 }
 
+// warp-aggregated reservation of k consecutive slots per calling lane: returns the first
+// slot, or -1 (and the overflow flag) when they do not all fit
+DT_D long long queue_reserve_n(const DevScene &sc, const Queue &q, unsigned k) {
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    const unsigned rank = __popc(mask & ((1u << lane) - 1u));
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(q.count, (unsigned long long)__popc(mask) * k);
+    base = __shfl_sync(mask, base, leader);
+    const unsigned long long slot = base + (unsigned long long)rank * k;
+    if (slot + k > q.cap) {
+        set_error(sc, ERR_QUEUE);
+        return -1;
+    }
+    return (long long)slot;
+}
+
 // camera.cpp:52-60 / 75-83 / 40-50
 DT_D void camera_ray(const DevCamera &cam, double x, double y, float3 &o, float3 &d) {
     const double sx = x / cam.width, sy = y / cam.height, aspect = (double)cam.width / cam.height;
@@ -699,12 +717,13 @@ __global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Q
             const double k2 = 1.0 / (pdf * rp.sppse);
 #pragma unroll
             for (int j = 0; j < N; ++j) s[j] = (float)((nrm.x * w1d[j][0] + nrm.y * w1d[j][1] + nrm.z * w1d[j][2]) * k2);
-            for (int sgn = 0; sgn < 2; ++sgn) {
+            // the two sub-paths of a sample in adjacent slots: k_li then traces the nearly
+            // identical rays (1e-4 rad apart) in neighbouring lanes of one warp
+            const long long slot = queue_reserve_n(sc, qli, 2);
+            for (int sgn = 0; sgn < 2 && slot >= 0; ++sgn) {
                 const double a = sgn == 0 ? -(double)kAngleEps : (double)kAngleEps;
                 const double3_ w2 = normalized(w1 + nrm * a);
-                const long long slot = queue_reserve(sc, qli);
-                if (slot < 0) continue;
-                LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot];
+                LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot + sgn];
                 t.o[0] = (float)x0.x; t.o[1] = (float)x0.y; t.o[2] = (float)x0.z;
                 t.d[0] = (float)w2.x; t.d[1] = (float)w2.y; t.d[2] = (float)w2.z;
                 const float sg = sgn == 0 ? 1.f : -1.f;
@@ -914,13 +933,12 @@ __global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp
             camera_ray(cam, ipx + fx, ipy + fy, o, d);
             const float tr = eval_transmittance(sc, stack, o, d, false, cam.med_id, maxd, rng, rp.max_bounces - 1, c);
             if (tr > kEps) {
-                for (int sgn = 0; sgn < 2; ++sgn) {
+                const long long slot = queue_reserve_n(sc, qli, 2);  // the pair in adjacent slots
+                for (int sgn = 0; sgn < 2 && slot >= 0; ++sgn) {
                     const double delta = sgn == 0 ? -1e-4 : 1e-4;
                     float3 o2, d2;
                     camera_ray(cam, ipx + fx + nx * delta, ipy + fy + ny * delta, o2, d2);
-                    const long long slot = queue_reserve(sc, qli);
-                    if (slot < 0) continue;
-                    LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot];
+                    LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot + sgn];
                     t.o[0] = o2.x; t.o[1] = o2.y; t.o[2] = o2.z;
                     t.d[0] = d2.x; t.d[1] = d2.y; t.d[2] = d2.z;
                     const float w = (float)(sgn == 0 ? rp.prim_weight : -rp.prim_weight);

@@ -377,12 +377,11 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
             const double nw = dotd(nrm, w1), k2 = 1.0 / (dist * pdf * rp.sppse);
             const double3_ m = (nrm - w1 * nw) * k2;
             const float3 c0 = tof(m * w0), c1 = tof(m * wb), cx = tof(m * (-(w0 + wb)));
-            for (int sgn = 0; sgn < 2; ++sgn) {
+            const long long slot = queue_reserve_n(sc, qli, 2);  // the pair in adjacent slots
+            for (int sgn = 0; sgn < 2 && slot >= 0; ++sgn) {
                 const double a = sgn == 0 ? -(double)kAngleEps : (double)kAngleEps;
                 const double3_ w2 = normalized(w1 + nrm * a);
-                const long long slot = queue_reserve(sc, qli);
-                if (slot < 0) continue;
-                VLiTask &t = reinterpret_cast<VLiTask *>(qli.data)[slot];
+                VLiTask &t = reinterpret_cast<VLiTask *>(qli.data)[slot + sgn];
                 t.o[0] = (float)x0.x; t.o[1] = (float)x0.y; t.o[2] = (float)x0.z;
                 t.d[0] = (float)w2.x; t.d[1] = (float)w2.y; t.d[2] = (float)w2.z;
                 const float sg = sgn == 0 ? 1.f : -1.f;
@@ -445,13 +444,12 @@ __global__ void __launch_bounds__(kBlock) k_vadj_primary(DevScene sc, RenderPara
             camera_ray(cam, ipx + fx, ipy + fy, o, d);
             const float tr = eval_transmittance(sc, stack, o, d, false, cam.med_id, maxd, rng, rp.max_bounces - 1, c);
             if (tr > kEps) {
-                for (int sgn = 0; sgn < 2; ++sgn) {
+                const long long slot = queue_reserve_n(sc, qli, 2);  // the pair in adjacent slots
+                for (int sgn = 0; sgn < 2 && slot >= 0; ++sgn) {
                     const double delta = sgn == 0 ? -1e-4 : 1e-4;
                     float3 o2, d2;
                     camera_ray(cam, ipx + fx + nx * delta, ipy + fy + ny * delta, o2, d2);
-                    const long long slot = queue_reserve(sc, qli);
-                    if (slot < 0) continue;
-                    VLiTask &t = reinterpret_cast<VLiTask *>(qli.data)[slot];
+                    VLiTask &t = reinterpret_cast<VLiTask *>(qli.data)[slot + sgn];
                     t.o[0] = o2.x; t.o[1] = o2.y; t.o[2] = o2.z;
                     t.d[0] = d2.x; t.d[1] = d2.y; t.d[2] = d2.z;
                     const float w = (float)(sgn == 0 ? rp.prim_weight : -rp.prim_weight);

@@ -436,13 +436,15 @@ int dtrt_batch_destroy(dtrt_batch *batch);
  * codes, radix sort, radix tree, bottom-up boxes; leaves of <= 4 triangles; updates build
  * it again), falling back to the host build when the tree would be deeper than the
  * traversal stack. DTRT_BVH_AUTO (default): the device build from
- * DTRT_BVH_DEVICE_MIN_TRIS triangles. The setting is process-wide and applies to scenes
+ * DTRT_BVH_DEVICE_MIN_TRIS triangles, where the host build time outweighs the device
+ * tree's slower traversal (its spatial-median splits visit more nodes per ray than the
+ * host's SAH splits). The setting is process-wide and applies to scenes
  * created or updated afterwards. Closest hits do not depend on the tree except at exact
  * ties. */
 #define DTRT_BVH_AUTO 0
 #define DTRT_BVH_HOST 1
 #define DTRT_BVH_DEVICE 2
-#define DTRT_BVH_DEVICE_MIN_TRIS 16384
+#define DTRT_BVH_DEVICE_MIN_TRIS 65536
 int dtrt_set_bvh_builder(int builder);
 
 typedef struct {

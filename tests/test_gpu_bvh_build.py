@@ -64,7 +64,7 @@ def test_device_tree_renders_like_the_host_tree(native):
 
 
 def test_device_tree_update_and_auto_choice(native):
-    spec = scenes.config2(16, 16, subdiv=5, nder=1)  # 20484 triangles: AUTO builds on the device
+    spec = scenes.config2(16, 16, subdiv=6, nder=1)  # 81924 triangles: AUTO builds on the device
     assert spec.num_triangles() >= _abi.BVH_DEVICE_MIN_TRIS
     with native.NativeScene(spec) as s:
         info = s.bvh_info()

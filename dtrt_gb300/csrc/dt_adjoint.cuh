@@ -213,11 +213,11 @@ DT_D bool replay_surface(const DevScene &sc, const RenderParams &rp, int *stack,
             const float3 e = ev[k];
             adj.w = dot(gpix, e) * rp.inv_spp;
             nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c,
-                              is_zero3(e, 0.f) ? nullptr : hook);
+                              is_zero3(e, 0.f) ? nullptr : hook, &b);
             acc = acc + e;
         } else {
             const Rng saved = rng;
-            DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+            DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c, nullptr, &b);
             float3 e = zero;
             if (!v.is_zero()) {
                 const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
@@ -230,7 +230,7 @@ DT_D bool replay_surface(const DevScene &sc, const RenderParams &rp, int *stack,
                 adj.w = dot(gpix, e) * rp.inv_spp;
                 DV<N> wo2;
                 float pdf2;
-                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook);
+                nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo2, pdf2, c, hook, &b);
                 rng = after;
             }
             if (!pass_b && k < kReplayEvents) ev[k] = e;

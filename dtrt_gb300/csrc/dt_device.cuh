@@ -1331,8 +1331,13 @@ DT_HEAVY DV<N> nee_point_ad(const DevScene &sc, int *stack, const DV<N> &p, cons
 
 // scene.cpp:493-524 (AD, from a surface; wo in the dual shading frame)
 template <int N>
+// With `bsdf` (a BSDF without derivative slots, whose value the caller multiplies in), a
+// light sample where that value is exactly zero returns zero before its visibility chain is
+// traced: the contribution is zero either way (a near-specular dielectric is zero for almost
+// every light sample). Random numbers such a chain would have drawn are not drawn.
 DT_HEAVY DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &its, const FrameAD<N> &fr, const float rnd[4],
-                          Rng &rng, int med, int max_inter, DV<N> &wo, float &pdf, Ctr &c, const AdjCtx *adj = nullptr) {
+                          Rng &rng, int med, int max_inter, DV<N> &wo, float &pdf, Ctr &c, const AdjCtx *adj = nullptr,
+                          const DevBsdf *bsdf = nullptr) {
     float3 lp, ln;
     float pdf0;
     const int l = sample_light(sc, rnd, lp, ln, pdf0);
@@ -1346,6 +1351,8 @@ DT_HEAVY DV<N> nee_surface_ad(const DevScene &sc, int *stack, const ItsAD<N> &it
         if (is_transition(s)) med = dot(dir, its.ng) > 0.f ? s.med_ext : s.med_int;
         const float dist = length(dir);
         dir = dir / dist;
+        if (bsdf && !bsdf->has_der && is_zero3(bsdf_eval(*bsdf, its.wi.val(), fr.plain().to_local(dir)), 0.f))
+            return DV<N>();
         ItsAD<N> near_its;
         int far_shape = -1;
         float far_t = 0.f;

@@ -368,7 +368,7 @@ DT_D bool camera_surface(const DevScene &sc, const RenderParams &rp, int *stack,
     DV<N> wo;
     float pdf_nee;
     if (!is_null && (mode & MODE_SURFACE_MAIN)) {
-        DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c);
+        DV<N> v = nee_surface_ad<N>(sc, stack, its, fr, r2, rng, med, depth - 1, wo, pdf_nee, c, nullptr, &b);
         if (!v.is_zero()) {
             const DV<N> bv = bsdf_eval_ad<N>(b, its.wi, wo);
             const float bp = bsdf_pdf(b, its0.wi, wo.val());

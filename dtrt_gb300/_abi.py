@@ -149,7 +149,7 @@ class BvhInfo(ctypes.Structure):
 
 
 BATCH_MAX_ITEMS, BATCH_MAX_TRIALS = 256, 16
-BATCH_AUTOTUNE, BATCH_GRAPH, BATCH_TUNE_FULL = 1, 2, 4
+BATCH_AUTOTUNE, BATCH_GRAPH, BATCH_TUNE_FULL, BATCH_WAVEFRONT = 1, 2, 4, 8
 
 
 class BatchItem(ctypes.Structure):
@@ -167,22 +167,29 @@ class BatchStats(ctypes.Structure):
         ("trial_ms", ctypes.c_float * BATCH_MAX_TRIALS), ("tune_sample_stride", ctypes.c_int64),
         ("full_ms", ctypes.c_float * 4),
         ("item_ms_estimate", ctypes.c_double * BATCH_MAX_ITEMS), ("order", ctypes.c_int * BATCH_MAX_ITEMS),
+        ("full_ms_wavefront", ctypes.c_float), ("wave_capacity", ctypes.c_int64),
     ]
 
     def as_dict(self):
         n, t = self.num_items, self.num_trials
+        names = {0: "persistent", 1: "per_item_launches", 2: "wavefront"}
+
+        def trial(c):
+            return "per_item_launches" if c < 0 else "wavefront" if c == 0 else "persistent"
         return {"num_items": n, "total_paths": self.total_paths, "grid_blocks": self.grid_blocks,
                 "blocks_per_sm": self.blocks_per_sm,
-                "schedule": "per_item_launches" if self.schedule == 1 else "persistent", "streams": self.streams,
+                "schedule": names.get(self.schedule, "?"), "streams": self.streams,
                 "chunk_paths": self.chunk_paths,
                 "order_longest_first": bool(self.order_longest_first), "graph": bool(self.graph),
-                "trials": [{"schedule": "per_item_launches" if self.trial_chunk[i] < 0 else "persistent",
+                "trials": [{"schedule": trial(self.trial_chunk[i]),
                             "chunk": max(self.trial_chunk[i], 0), "streams": max(-self.trial_chunk[i], 1),
                             "order": "longest_first" if self.trial_order[i] == 0 else "input",
                             "ms": self.trial_ms[i]} for i in range(t)],
                 "tune_sample_stride": self.tune_sample_stride,
                 "full_size_ms": {"persistent": self.full_ms[0], "per_item_1": self.full_ms[1],
-                                 "per_item_2": self.full_ms[2], "per_item_4": self.full_ms[3]},
+                                 "per_item_2": self.full_ms[2], "per_item_4": self.full_ms[3],
+                                 "wavefront": self.full_ms_wavefront},
+                "wave_capacity": self.wave_capacity,
                 "item_ms_estimate": list(self.item_ms_estimate[:min(n, BATCH_MAX_ITEMS)]),
                 "order": list(self.order[:min(n, BATCH_MAX_ITEMS)])}
 

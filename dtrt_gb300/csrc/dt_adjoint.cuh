@@ -491,4 +491,139 @@ static __global__ void k_adjoint_image(int npix, const double *acc, float *out) 
     for (int c = 0; c < 3; ++c) out[(size_t)p * 3 + c] = nonneg ? (float)a[c] : 0.f;
 }
 
+// ====================================================================== batched wavefront
+// The replay of many scenes as one wavefront (batch schedule of dt_batch.cu): the camera
+// paths of all items are numbered item after item (gbeg[i]: the first global path of the
+// i-th item of `order`), a workspace of `count` consecutive global paths runs pass A and
+// pass B as above, and every level launch covers the live paths of all items at once. A
+// thread finds its path's item by binary search over gbeg and reads that item's scene and
+// parameters from global memory. With stride > 1 (tuning), global path k of an item is
+// its path k * stride.
+struct BatchItemDev {
+    DevScene sc;
+    RenderParams rp;
+    const float *dimg;
+    float *grad;
+    double *img_acc;
+};
+
+struct BatchWave {
+    const BatchItemDev *items;
+    const long long *gbeg;  // n + 1 entries
+    const int *order;
+    int n;
+    long long begin, count;  // global paths of this workspace: [begin, begin + count)
+    long long stride;
+};
+
+// item of workspace slot i and its local path index
+DT_D const BatchItemDev &batch_item(const BatchWave &bw, long long i, long long &g) {
+    const long long G = bw.begin + i;
+    int lo = 0, hi = bw.n - 1;  // largest position with gbeg <= G
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (bw.gbeg[mid] <= G) lo = mid;
+        else hi = mid - 1;
+    }
+    g = (G - bw.gbeg[lo]) * bw.stride;
+    return bw.items[bw.order[lo]];
+}
+
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_badj_start(BatchWave bw, AdjState<N> *states, VertexIn<N> *vins, int *qv0,
+                                                       unsigned long long *cnt_v0, int *qv1,
+                                                       unsigned long long *cnt_v1, int *qs1,
+                                                       unsigned long long *cnt_s1, const float3 *totals,
+                                                       float3 *evbuf, bool pass_b) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < bw.count;
+    long long g = 0;
+    const BatchItemDev &it = batch_item(bw, active ? gi : 0, g);
+    Ctr c;
+    int kind = 0;
+    bool next = false, run = false;
+    AdjState<N> st;
+    const float3 zero = mk(0.f, 0.f, 0.f);
+    float3 total = zero, gp = zero;
+    AdjCtx adj{it.grad, 0.f};
+    if (active) {
+        if (pass_b && it.grad) {
+            total = totals[gi];
+            gp = pixel_dldi(it.rp, it.dimg, g);
+        }
+        run = !pass_b || (it.grad && !is_zero3(total, 0.f) && !is_zero3(gp, 0.f));
+        if (run && replay_start<N>(it.sc, it.rp, stack, g, st, c) && st.mode != 0) {
+            VertexIn<N> vin;
+            kind = replay_decide<N>(it.sc, it.rp, pass_b, total, gp, adj, c, st, vin);
+            if (kind == 1) vins[gi] = vin;
+            if (kind == 2) {
+                next = replay_surface<N>(it.sc, it.rp, stack, pass_b, gp, adj, c, evbuf + (size_t)gi * kReplayEvents,
+                                         st, vin);
+                ++st.level;
+            }
+        }
+    }
+    push_path(qv0, cnt_v0, (int)gi, kind == 1);
+    replay_next<N>(it.sc, it.rp, st, next, pass_b, total, gp, adj, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    if (run) states[gi] = st;
+}
+
+template <int N, bool kVolume>
+__global__ void __launch_bounds__(kBlock) k_badj_vertex(BatchWave bw, AdjState<N> *states, VertexIn<N> *vins,
+                                                        const int *q_in, const unsigned long long *cnt_in,
+                                                        int *qv_next, unsigned long long *cnt_v_next, int *qs_next,
+                                                        unsigned long long *cnt_s_next, const float3 *totals,
+                                                        float3 *evbuf, bool pass_b) {
+    __shared__ int s_stack[kStackDepth * kBlock];
+    int *stack = s_stack + threadIdx.x;
+    const long long n = (long long)*cnt_in;
+    Ctr c;
+    for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
+        const int id = q_in[i];
+        long long g;
+        const BatchItemDev &it = batch_item(bw, id, g);
+        AdjState<N> st = states[id];
+        const VertexIn<N> vin = vins[id];
+        const float3 zero = mk(0.f, 0.f, 0.f);
+        const float3 total = pass_b ? totals[id] : zero, gp = pass_b ? pixel_dldi(it.rp, it.dimg, g) : zero;
+        AdjCtx adj{it.grad, 0.f};
+        float3 *ev = evbuf + (size_t)id * kReplayEvents;
+        const bool alive = kVolume ? replay_volume<N>(it.sc, it.rp, stack, pass_b, gp, adj, c, ev, st, vin)
+                                   : replay_surface<N>(it.sc, it.rp, stack, pass_b, gp, adj, c, ev, st, vin);
+        ++st.level;
+        replay_next<N>(it.sc, it.rp, st, alive, pass_b, total, gp, adj, vins, id, qv_next, cnt_v_next, qs_next,
+                       cnt_s_next, c);
+        states[id] = st;
+    }
+}
+
+// after pass A: each path's value and its item's image sum (a warp whose lanes share one
+// item and pixel reduces with shuffles first)
+template <int N>
+__global__ void __launch_bounds__(kBlock) k_badj_totals(BatchWave bw, const AdjState<N> *states, float3 *totals) {
+    const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
+    const bool active = gi < bw.count;
+    long long g = 0;
+    const BatchItemDev &it = batch_item(bw, active ? gi : 0, g);
+    const int pixel = (int)(g / it.rp.spp);
+    float3 total = mk(0.f, 0.f, 0.f);
+    if (active) {
+        total = states[gi].acc;
+        totals[gi] = total;
+    }
+    const unsigned full = 0xffffffffu;
+    const unsigned long long key = ((unsigned long long)(&it - bw.items) << 32) | (unsigned)pixel;
+    const unsigned long long k0 = __shfl_sync(full, key, 0);
+    const bool uniform = __all_sync(full, active && key == k0);
+    float v[3] = {total.x * it.rp.inv_spp, total.y * it.rp.inv_spp, total.z * it.rp.inv_spp};
+    if (uniform)
+        for (int k = 0; k < 3; ++k)
+            for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(full, v[k], off);
+    if (active && it.img_acc && (!uniform || (threadIdx.x & 31) == 0))
+        for (int k = 0; k < 3; ++k)
+            if (v[k] != 0.f) atomicAdd(it.img_acc + (size_t)pixel * 3 + k, (double)v[k]);
+}
+
 }  // namespace dt

@@ -29,14 +29,6 @@
 
 namespace dt {
 
-struct BatchItemDev {
-    DevScene sc;
-    RenderParams rp;
-    const float *dimg;
-    float *grad;
-    double *img_acc;
-};
-
 // chunk c belongs to the item at position i of the order with cbeg[i] <= c < cbeg[i+1]
 __global__ void __launch_bounds__(kBlock) k_batch(const BatchItemDev *items, const long long *cbeg, const int *order,
                                                   int n, long long total_chunks, int chunk, long long sample_stride,
@@ -130,7 +122,8 @@ struct dtrt_batch {
     long long total_chunks = 0, total_pix = 0;
     std::vector<int> order;
     std::vector<long long> cbeg;
-    // schedule: 0 persistent launch, 1 one launch per item spread over `nstreams` streams
+    // schedule: 0 persistent launch, 1 one launch per item spread over `nstreams` streams,
+    // 2 one wavefront over all items
     int schedule = 0, nstreams = 1;
     std::vector<cudaStream_t> side;  // streams 1.. of the per-item schedule
     std::vector<cudaEvent_t> side_ev;
@@ -138,6 +131,14 @@ struct dtrt_batch {
     // wavefront replay workspaces of the per-item schedule, one per stream (empty: megakernel)
     std::vector<void *> wave_mem;
     std::vector<dt::AdjWave> wave;
+    // the batch wavefront (schedule 2): one replay wavefront over the paths of all items
+    void *bw_mem = nullptr;
+    dt::AdjWave bw;
+    int max_levels = 1;
+    bool any_grad = false;
+    // tuning: best strided-sample time of the persistent launch, the per-item schedule on
+    // 1, 2 and 4 streams, and the batch wavefront
+    float sampled_best[5] = {1e30f, 1e30f, 1e30f, 1e30f, 1e30f};
     int sms = 0;
     // graph
     cudaStream_t cap_stream = nullptr;
@@ -148,6 +149,9 @@ struct dtrt_batch {
 
 namespace dt {
 namespace {
+
+// paths per workspace of the batch wavefront (about 780 B of replay state per path)
+constexpr long long kBatchWaveCap = 1ll << 23;
 
 #define DT_BCK(call)                                                                 \
     do {                                                                             \
@@ -166,6 +170,7 @@ void free_batch(dtrt_batch *b) {
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     for (void *p : b->wave_mem) cudaFree(p);
+    if (b->bw_mem) cudaFree(b->bw_mem);
     void *ptrs[] = {b->d_items, b->d_cbeg, b->d_order, b->d_imgs, b->d_next, b->d_err};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -248,8 +253,89 @@ int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long 
     return DTRT_OK;
 }
 
+// the batch wavefront's path numbering: items in `order`, every stride-th path (blocking
+// copies: never inside a stream capture). Returns the number of global paths.
+int upload_wave_layout(dtrt_batch *b, const std::vector<int> &order, long long stride, long long &total) {
+    std::vector<long long> gbeg(b->n + 1, 0);
+    for (int i = 0; i < b->n; ++i) gbeg[i + 1] = gbeg[i] + (b->paths[order[i]] + stride - 1) / stride;
+    total = gbeg[b->n];
+    DT_BCK(cudaMemcpy(b->d_cbeg, gbeg.data(), gbeg.size() * 8, cudaMemcpyHostToDevice));
+    DT_BCK(cudaMemcpy(b->d_order, order.data(), order.size() * 4, cudaMemcpyHostToDevice));
+    return DTRT_OK;
+}
+
+// One replay wavefront over the uploaded numbering, in chunks of a workspace's capacity:
+// pass A (start, one launch per vertex kind and level, totals), then, when an item asks
+// for a density gradient, pass B. Every level launch covers live paths of all items; a
+// chunk spans item boundaries. Chunks are independent: they are dealt round-robin to the
+// caller's stream and the side streams, each with its own workspace, so that one chunk's
+// last, sparse levels overlap the next chunk's work.
+int enqueue_chunk(dtrt_batch *b, const AdjWave &w, BatchWave bw, cudaStream_t st) {
+    const int levels = b->max_levels;
+    auto blocks = [](long long n) { return (unsigned)((n + kBlock - 1) / kBlock); };
+    AdjState<1> *states = (AdjState<1> *)w.states;
+    VertexIn<1> *vins = (VertexIn<1> *)w.vins;
+    int *qa = w.q, *qb = qa + w.cap, *qv = qb + w.cap, *qs = qv + w.cap;
+    {
+        const unsigned gw = std::min<unsigned>(blocks(bw.count), (unsigned)std::max(1, b->sms) * 16u);
+        DT_BCK(cudaMemsetAsync(w.cnt, 0, (size_t)4 * (levels + 1) * sizeof(unsigned long long), st));
+        for (int pass = 0; pass < (b->any_grad ? 2 : 1); ++pass) {
+            const bool pb = pass == 1;
+            unsigned long long *vc = w.cnt + pass * 2 * (levels + 1), *scn = vc + (levels + 1);
+            k_badj_start<1><<<blocks(bw.count), kBlock, 0, st>>>(bw, states, vins, qa, vc, qv, vc + 1, qs, scn + 1,
+                                                                w.tots, w.ev, pb);
+            for (int L = 0; L < levels; ++L) {
+                int *qvl = (L & 1) ? qv : qa, *qsl = (L & 1) ? qs : qb;
+                int *qvn = (L & 1) ? qa : qv, *qsn = (L & 1) ? qb : qs;
+                k_badj_vertex<1, true><<<gw, kBlock, 0, st>>>(bw, states, vins, qvl, vc + L, qvn, vc + L + 1, qsn,
+                                                             scn + L + 1, w.tots, w.ev, pb);
+                if (L > 0)
+                    k_badj_vertex<1, false><<<gw, kBlock, 0, st>>>(bw, states, vins, qsl, scn + L, qvn, vc + L + 1,
+                                                                  qsn, scn + L + 1, w.tots, w.ev, pb);
+            }
+            if (pass == 0) k_badj_totals<1><<<blocks(bw.count), kBlock, 0, st>>>(bw, states, w.tots);
+        }
+        DT_BCK(cudaGetLastError());
+    }
+    return DTRT_OK;
+}
+
+int enqueue_wave(dtrt_batch *b, long long total, long long stride, cudaStream_t st) {
+    // workspaces: the per-stream ones of the per-item schedule when they hold the deepest
+    // item's levels, else the single batch workspace
+    const bool multi = b->wave.size() == 4 && b->wave[0].levels >= b->max_levels;
+    const int S = multi ? 4 : 1;
+    const long long cap = multi ? b->wave[0].cap : b->bw.cap;
+    if (S > 1) {
+        DT_BCK(cudaEventRecord(b->fork_ev, st));
+        for (int k = 1; k < S; ++k) DT_BCK(cudaStreamWaitEvent(b->side[k - 1], b->fork_ev, 0));
+    }
+    BatchWave bw{b->d_items, b->d_cbeg, b->d_order, b->n, 0, 0, stride};
+    int k = 0;
+    for (long long b0 = 0; b0 < total; b0 += cap, k = (k + 1) % S) {
+        bw.begin = b0;
+        bw.count = std::min(cap, total - b0);
+        cudaStream_t q = k == 0 ? st : b->side[k - 1];
+        int rc = enqueue_chunk(b, multi ? b->wave[k] : b->bw, bw, q);
+        if (rc) return rc;
+    }
+    for (int j = 1; j < S; ++j) {
+        DT_BCK(cudaEventRecord(b->side_ev[j - 1], b->side[j - 1]));
+        DT_BCK(cudaStreamWaitEvent(st, b->side_ev[j - 1], 0));
+    }
+    return DTRT_OK;
+}
+
+int launch_wave(dtrt_batch *b, const std::vector<int> &order, long long stride, cudaStream_t st) {
+    long long total = 0;
+    DT_BCK(cudaStreamSynchronize(st));  // the numbering buffers may still be read by a previous launch
+    int rc = upload_wave_layout(b, order, stride, total);
+    return rc ? rc : enqueue_wave(b, total, stride, st);
+}
+
 int launch_schedule(dtrt_batch *b, cudaStream_t st, long long stride) {
     if (b->schedule == 1) return launch_items(b, b->order, b->nstreams, stride, st, true);
+    if (b->schedule == 2) return launch_wave(b, b->order, stride, st);
     return launch_once(b, b->order, b->chunk, stride, st);
 }
 
@@ -343,6 +429,7 @@ int autotune(dtrt_batch *b, cudaStream_t st) {
             }
         }
     }
+    b->sampled_best[0] = best;
     // one launch per item over 1, 2 or 4 streams (longest first)
     for (int S : {1, 2, 4}) {
         float ms = 0.f;
@@ -355,6 +442,7 @@ int autotune(dtrt_batch *b, cudaStream_t st) {
             b->stats.trial_ms[trial] = ms;
         }
         ++trial;
+        b->sampled_best[S == 1 ? 1 : S == 2 ? 2 : 3] = ms;
         if (ms < best) {
             best = ms;
             b->schedule = 1;
@@ -363,15 +451,35 @@ int autotune(dtrt_batch *b, cudaStream_t st) {
             b->stats.order_longest_first = 1;
         }
     }
+    // one wavefront over all items (input order)
+    if (b->bw_mem) {
+        float ms = 0.f;
+        DT_BCK(cudaStreamSynchronize(st));
+        int rc = timed(st, [&]() { return launch_wave(b, natural, stride, st); }, ms);
+        if (rc) return rc;
+        if (trial < DTRT_BATCH_MAX_TRIALS) {
+            b->stats.trial_chunk[trial] = 0;  // 0: the batch wavefront
+            b->stats.trial_order[trial] = 1;
+            b->stats.trial_ms[trial] = ms;
+        }
+        ++trial;
+        b->sampled_best[4] = ms;
+        if (ms < best) {
+            best = ms;
+            b->schedule = 2;
+            b->order = natural;
+            b->stats.order_longest_first = 0;
+        }
+    }
     b->stats.num_trials = std::min(trial, DTRT_BATCH_MAX_TRIALS);
     b->stats.tune_sample_stride = stride;
     return DTRT_OK;
 }
 
 // Full-size confirmation (DTRT_BATCH_TUNE_FULL): a strided sample shrinks every per-item
-// launch to a few waves, which understates that schedule on large items. Time the sampled
-// winner of the persistent schedule and the per-item schedule on 1, 2 and 4 streams on the
-// whole batch once each and keep the fastest.
+// launch to a few waves, which understates that schedule on large items. The two
+// candidates (persistent, per-item on 1, 2 or 4 streams, batch wavefront) that were
+// fastest on the sample run once each on the whole batch; the faster one is kept.
 int autotune_full(dtrt_batch *b, cudaStream_t st) {
     const int saved_chunk = b->chunk;
     const std::vector<int> saved_order = b->order;
@@ -383,11 +491,31 @@ int autotune_full(dtrt_batch *b, cudaStream_t st) {
     });
     float best = 1e30f;
     int best_sched = 0, best_streams = 1;
-    for (int cand = 0; cand < 4; ++cand) {
+    std::vector<int> natural(b->n);
+    std::iota(natural.begin(), natural.end(), 0);
+    // the two best candidates on the strided sample are confirmed at full size. With items
+    // large enough for the wavefront replay the persistent megakernel is left out: the
+    // strided sample understates the wavefront schedules (a sample of a large item is a few
+    // short launches) and overstates the megakernel, which the replay wavefront outpaces
+    // several times at full size (7.3 s against 1.86 s on the 64-scene C4 batch)
+    std::vector<int> rank;
+    for (int cand = 0; cand < 5; ++cand)
+        if (!(cand == 0 && !b->wave.empty()) && !(cand == 4 && !b->bw_mem)) rank.push_back(cand);
+    std::stable_sort(rank.begin(), rank.end(), [&](int a, int c) { return b->sampled_best[a] < b->sampled_best[c]; });
+    rank.resize(std::max<size_t>(rank.size(), 2), -1);
+    for (int cand = 0; cand < 5; ++cand) {
+        if (cand == 4 && !b->bw_mem) continue;
+        if (cand != rank[0] && cand != rank[1]) {
+            if (cand < 4) b->stats.full_ms[cand] = -1.f;
+            else b->stats.full_ms_wavefront = -1.f;
+            continue;
+        }
         float ms = 0.f;
         DT_BCK(cudaStreamSynchronize(st));
         int rc;
-        if (cand == 0) {
+        if (cand == 4) {
+            rc = timed(st, [&]() { return launch_wave(b, natural, 1, st); }, ms);
+        } else if (cand == 0) {
             long long total = 0;
             rc = upload_layout(b, saved_order, saved_chunk, 1, total);
             if (rc) return rc;
@@ -396,18 +524,19 @@ int autotune_full(dtrt_batch *b, cudaStream_t st) {
             rc = timed(st, [&]() { return launch_items(b, longest, 1 << (cand - 1), 1, st); }, ms);
         }
         if (rc) return rc;
-        b->stats.full_ms[cand] = ms;
+        if (cand < 4) b->stats.full_ms[cand] = ms;
+        else b->stats.full_ms_wavefront = ms;
         if (ms < best) {
             best = ms;
-            best_sched = cand == 0 ? 0 : 1;
-            best_streams = cand == 0 ? 1 : 1 << (cand - 1);
+            best_sched = cand == 0 ? 0 : cand == 4 ? 2 : 1;
+            best_streams = (cand == 0 || cand == 4) ? 1 : 1 << (cand - 1);
         }
     }
     b->schedule = best_sched;
     b->nstreams = best_streams;
     b->chunk = saved_chunk;
-    b->order = best_sched == 0 ? saved_order : longest;
-    b->stats.order_longest_first = best_sched == 1 ? 1 : b->stats.order_longest_first;
+    b->order = best_sched == 0 ? saved_order : best_sched == 2 ? natural : longest;
+    b->stats.order_longest_first = best_sched == 1 ? 1 : best_sched == 2 ? 0 : b->stats.order_longest_first;
     return DTRT_OK;
 }
 
@@ -416,12 +545,13 @@ int autotune_full(dtrt_batch *b, cudaStream_t st) {
 int capture(dtrt_batch *b) {
     cudaStream_t cs = b->cap_stream;
     long long total = 0;
-    int rc = upload_layout(b, b->order, b->chunk, 1, total);
+    int rc = b->schedule == 2 ? upload_wave_layout(b, b->order, 1, total) : upload_layout(b, b->order, b->chunk, 1, total);
     if (rc) return rc;
     DT_BCK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     rc = zero_outputs(b, cs);
     if (!rc) rc = b->schedule == 1 ? launch_items(b, b->order, b->nstreams, 1, cs, true)
-                                   : launch_kernel(b, total, b->chunk, 1, cs);
+                  : b->schedule == 2 ? enqueue_wave(b, total, 1, cs)
+                                     : launch_kernel(b, total, b->chunk, 1, cs);
     if (!rc && b->n_img > 0) {
         k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, cs>>>(b->d_imgs, b->n_img, b->total_pix);
         if (cudaGetLastError() != cudaSuccess) rc = DTRT_ERR_CUDA;
@@ -578,12 +708,34 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
             }
         }
     }
+    // workspace of the batch wavefront: one replay wavefront over the paths of all items
+    {
+        long long tp = 0;
+        for (int i = 0; i < n; ++i) {
+            tp += b->paths[i];
+            b->max_levels = std::max(b->max_levels, items[i].opts.max_bounces + 1);
+            b->any_grad = b->any_grad || b->host_items[i].grad != nullptr;
+        }
+        const long long cap = std::max<long long>(1, std::min<long long>(kBatchWaveCap, tp));
+        if (cudaMalloc(&b->bw_mem, AdjWave::bytes(cap, b->max_levels)) == cudaSuccess) {
+            b->bw.carve(b->bw_mem, cap, b->max_levels);
+        } else {
+            cudaGetLastError();  // no room: the other schedules only
+            b->bw_mem = nullptr;
+        }
+    }
     b->order.resize(n);
     std::iota(b->order.begin(), b->order.end(), 0);
     b->chunk = 128;
     b->stats.grid_blocks = b->grid;
     b->stats.blocks_per_sm = per_sm;
-    if (flags & (DTRT_BATCH_AUTOTUNE | DTRT_BATCH_TUNE_FULL)) {
+    if (flags & DTRT_BATCH_WAVEFRONT) {
+        if (!b->bw_mem) {
+            set_last_error("batch wavefront: no device memory for its workspace");
+            return DTRT_ERR_CUDA;
+        }
+        b->schedule = 2;
+    } else if (flags & (DTRT_BATCH_AUTOTUNE | DTRT_BATCH_TUNE_FULL)) {
         int rc = autotune(b.get(), st);
         if (!rc && (flags & DTRT_BATCH_TUNE_FULL)) rc = autotune_full(b.get(), st);
         if (rc) return rc;
@@ -592,6 +744,7 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
     b->stats.chunk_paths = b->chunk;
     b->stats.schedule = b->schedule;
     b->stats.streams = b->schedule == 1 ? b->nstreams : 1;
+    b->stats.wave_capacity = b->bw_mem ? b->bw.cap : 0;
     for (int i = 0; i < n && i < DTRT_BATCH_MAX_ITEMS; ++i) b->stats.order[i] = b->order[i];
     b->stats.num_items = n;
     long long tp = 0;

@@ -205,12 +205,13 @@ class NativeScene:
 
 
 class Batch:
-    """Many scenes in one persistent launch (dtrt_batch_create / _launch / _destroy).
+    """Many scenes rendered together (dtrt_batch_create / _launch / _destroy): a persistent
+    launch, per-item launches over streams, or one replay wavefront over all items.
 
     items: list of (NativeScene, options, d_image_ptr, image_ptr, d_density_ptr) with
     device pointers as ints (0 = none). The scenes and buffers must outlive the batch."""
 
-    def __init__(self, items, autotune=True, graph=True, stream=None, tune_full=False):
+    def __init__(self, items, autotune=True, graph=True, stream=None, tune_full=False, wavefront=False):
         self.lib = _abi.load()
         self.scenes = [it[0] for it in items]  # keep the scenes alive
         arr = (_abi.BatchItem * len(items))()
@@ -221,7 +222,7 @@ class Batch:
             arr[i].image = img or None
             arr[i].d_density = dden or None
         flags = (_abi.BATCH_AUTOTUNE if autotune else 0) | (_abi.BATCH_GRAPH if graph else 0) | \
-            (_abi.BATCH_TUNE_FULL if tune_full else 0)
+            (_abi.BATCH_TUNE_FULL if tune_full else 0) | (_abi.BATCH_WAVEFRONT if wavefront else 0)
         h = ctypes.c_void_p()
         _abi.check(self.lib.dtrt_batch_create(arr, len(items), flags, ctypes.c_void_p(stream or 0), ctypes.byref(h)))
         self.handle = h

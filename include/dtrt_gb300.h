@@ -397,6 +397,7 @@ typedef struct {
 #define DTRT_BATCH_AUTOTUNE 1u /* measure item costs and pick item order and chunk size */
 #define DTRT_BATCH_GRAPH 2u    /* capture the launch in a CUDA graph */
 #define DTRT_BATCH_TUNE_FULL 4u /* also time the candidate schedules once each on the whole batch */
+#define DTRT_BATCH_WAVEFRONT 8u /* one replay wavefront over the paths of all items, without tuning */
 #define DTRT_BATCH_MAX_ITEMS 256
 #define DTRT_BATCH_MAX_TRIALS 16
 
@@ -404,7 +405,7 @@ typedef struct {
     int num_items;
     uint64_t total_paths;
     int grid_blocks, blocks_per_sm; /* persistent grid: resident blocks only */
-    int schedule;                   /* 0: persistent launch, 1: one launch per item */
+    int schedule;                   /* 0: persistent launch, 1: one launch per item, 2: one wavefront over all items */
     int streams;                    /* streams of the per-item schedule */
     int chunk_paths;                /* paths a warp takes per counter increment (schedule 0) */
     int order_longest_first;        /* 1: items ordered by measured cost, longest first */
@@ -412,11 +413,15 @@ typedef struct {
     int num_trials;
     int trial_chunk[DTRT_BATCH_MAX_TRIALS], trial_order[DTRT_BATCH_MAX_TRIALS];
     float trial_ms[DTRT_BATCH_MAX_TRIALS]; /* tuning launches on a strided path sample;
-                                              trial_chunk < 0: per-item schedule on -chunk streams */
+                                              trial_chunk < 0: per-item schedule on -chunk streams,
+                                              trial_chunk == 0: the batch wavefront */
     int64_t tune_sample_stride;
-    float full_ms[4];               /* DTRT_BATCH_TUNE_FULL: persistent, per-item on 1, 2, 4 streams */
+    float full_ms[4];               /* DTRT_BATCH_TUNE_FULL: persistent, per-item on 1, 2, 4 streams
+                                       (-1: not confirmed; the two best on the strided sample are) */
     double item_ms_estimate[DTRT_BATCH_MAX_ITEMS]; /* measured cost of each item (probe) */
     int order[DTRT_BATCH_MAX_ITEMS];
+    float full_ms_wavefront;        /* DTRT_BATCH_TUNE_FULL: the batch wavefront (-1: not confirmed) */
+    int64_t wave_capacity;          /* paths per workspace of the batch wavefront (0: not available) */
 } dtrt_batch_stats;
 
 typedef struct dtrt_batch dtrt_batch;

@@ -1,7 +1,7 @@
-"""Batches of uneven scenes in one persistent launch (dtrt_batch_*): every item's image and
-density gradient equal the single-scene adjoint render of the same options (up to the
-order of floating-point atomic adds), with and without autotuning and graph capture, and
-across repeated launches."""
+"""Batches of uneven scenes (dtrt_batch_*): every item's image and density gradient equal the
+single-scene adjoint render of the same options (up to the order of floating-point atomic
+adds), with and without autotuning and graph capture, under the batch wavefront (one replay
+wavefront over the paths of all items), and across repeated launches."""
 import numpy as np
 import pytest
 
@@ -36,17 +36,21 @@ def _single(it, torch):
     return img.cpu().numpy(), grad.cpu().numpy()
 
 
-@pytest.mark.parametrize("autotune,graph", [(True, True), (False, False), (False, True)])
-def test_batch_matches_single_renders(native, autotune, graph):
+@pytest.mark.parametrize("autotune,graph,wavefront", [(True, True, False), (False, False, False),
+                                                     (False, True, False), (False, False, True),
+                                                     (False, True, True)])
+def test_batch_matches_single_renders(native, autotune, graph, wavefront):
     torch = pytest.importorskip("torch")
     items = _items(native, torch)
     assert any(it["nvox"] for it in items) and any(not it["nvox"] for it in items)
     ref = [_single(it, torch) for it in items]
     batch = native.Batch([(it["scene"], it["opts"], it["dimg"].data_ptr(), it["img"].data_ptr(),
                            it["grad"].data_ptr() if it["nvox"] else 0) for it in items], autotune=autotune,
-                         graph=graph, stream=torch.cuda.current_stream().cuda_stream)
+                         graph=graph, stream=torch.cuda.current_stream().cuda_stream, wavefront=wavefront)
     st = batch.stats()
     assert st["num_items"] == len(items) and st["graph"] == graph
+    if wavefront:
+        assert st["schedule"] == "wavefront" and st["wave_capacity"] > 0
     if autotune:
         assert len(st["trials"]) >= 2
         assert sorted(st["order"]) == list(range(len(items)))
@@ -64,6 +68,29 @@ def test_batch_matches_single_renders(native, autotune, graph):
     batch.close()
     for it in items:
         it["scene"].close()
+
+
+def test_batch_wavefront_single_item(native):
+    """A batch wavefront over one item is that item's replay wavefront."""
+    torch = pytest.importorskip("torch")
+    items = _items(native, torch)
+    it = next(x for x in items if x["nvox"])
+    for x in items:
+        if x is not it:
+            x["scene"].close()
+    img_r, grad_r = _single(it, torch)
+    batch = native.Batch([(it["scene"], it["opts"], it["dimg"].data_ptr(), it["img"].data_ptr(),
+                           it["grad"].data_ptr())], autotune=False, graph=False,
+                         stream=torch.cuda.current_stream().cuda_stream, wavefront=True)
+    assert batch.stats()["schedule"] == "wavefront"
+    batch.launch(stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    img = it["img"].cpu().numpy()
+    g = it["grad"].cpu().numpy()
+    assert np.abs(img - img_r).max() <= 1e-5 * max(1e-3, np.abs(img_r).max())
+    assert np.abs(g - grad_r).max() <= 1e-4 * max(1e-12, np.abs(grad_r).max()) and np.abs(g).max() > 0
+    batch.close()
+    it["scene"].close()
 
 
 def test_batch_rejects_bad_items(native):

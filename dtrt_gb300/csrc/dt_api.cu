@@ -394,6 +394,14 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
     cam.med_id = c.med_id;
     cam.clip_near = c.clip_near;
     cam.fov = (float)c2ndc[0];
+    {
+        const double aspect = (double)c.width / c.height, fov = (double)cam.fov;
+        cam.inv_w = 1.0 / c.width;
+        cam.inv_h = 1.0 / c.height;
+        cam.ndc_ky = -2.0 / aspect;
+        cam.plane_kx = 2.0 / fov;
+        cam.plane_ky = -2.0 / (aspect * fov);
+    }
     const bool cropped = c.crop_width > 0 && c.crop_height > 0;
     cam.crop_x = cropped ? c.crop_offset_x : 0;
     cam.crop_y = cropped ? c.crop_offset_y : 0;
@@ -574,7 +582,8 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
         double acc = 0;
         for (size_t k = 0; k < lens.size(); ++k) {
             acc += lens[k];
-            edge_cdf.push_back(k + 1 == lens.size() ? 1.0 : acc / sum);
+            // non-negative entries (no NaN): the device search compares their bit patterns
+            edge_cdf.push_back(k + 1 == lens.size() ? 1.0 : (sum > 0 ? acc / sum : 0.0));
         }
         s->shape_edge_len[si] = (float)sum;
         s->shape_skip[si] = 0;
@@ -893,6 +902,14 @@ int build_scene(dtrt_scene *s, const dtrt_scene_desc *d, Builder &bld, bool rebu
             double *dsts[4] = {pe.v0p, pe.v1p, pe.v0c, pe.v1c};
             for (int q = 0; q < 4; ++q)
                 for (int a = 0; a < 3; ++a) dsts[q][a] = srcs[q][a];
+            {
+                const double nx = pe.v1s[1] - pe.v0s[1], ny = pe.v0s[0] - pe.v1s[0], nl = std::sqrt(nx * nx + ny * ny);
+                pe.n[0] = nx / nl;
+                pe.n[1] = ny / nl;
+                pe.inv_lenp = 1.0 / dnorm(sub(v1p, v0p));
+                pe.cb = dnorm(v0p) / dnorm(v0l);
+                pe.cc = dnorm(v1p) / dnorm(v1l);
+            }
             po.pe = pe;
             // Jacobian of the two clipped screen endpoints (pixels) w.r.t. the edge's vertex
             // positions (dual slots 0-2: v0, 3-5: v1) for a static camera: the same near-plane

@@ -134,8 +134,7 @@ DT_D long long queue_reserve_n(const DevScene &sc, const Queue &q, unsigned k) {
 
 // camera.cpp:52-60 / 75-83 / 40-50
 DT_D void camera_ray(const DevCamera &cam, double x, double y, float3 &o, float3 &d) {
-    const double sx = x / cam.width, sy = y / cam.height, aspect = (double)cam.width / cam.height;
-    const float3 ndc = mk((float)((sx - 0.5) * 2.0), (float)((sy - 0.5) * (-2.0) / aspect), 1.f);
+    const float3 ndc = mk((float)((x * cam.inv_w - 0.5) * 2.0), (float)((y * cam.inv_h - 0.5) * cam.ndc_ky), 1.f);
     const float *m = cam.ndc2cam;
     float3 dc = normalize(mk(m[0] * ndc.x + m[1] * ndc.y + m[2] * ndc.z, m[3] * ndc.x + m[4] * ndc.y + m[5] * ndc.z,
                              m[6] * ndc.x + m[7] * ndc.y + m[8] * ndc.z));
@@ -146,8 +145,7 @@ DT_D void camera_ray(const DevCamera &cam, double x, double y, float3 &o, float3
 }
 template <int N>
 DT_D RayAD<N> camera_ray_ad(const DevCamera &cam, double x, double y) {
-    const double sx = x / cam.width, sy = y / cam.height, aspect = (double)cam.width / cam.height;
-    const float3 ndc = mk((float)((sx - 0.5) * 2.0), (float)((sy - 0.5) * (-2.0) / aspect), 1.f);
+    const float3 ndc = mk((float)((x * cam.inv_w - 0.5) * 2.0), (float)((y * cam.inv_h - 0.5) * cam.ndc_ky), 1.f);
     const float *m = cam.ndc2cam;
     const float3 dc = normalize(mk(m[0] * ndc.x + m[1] * ndc.y + m[2] * ndc.z,
                                    m[3] * ndc.x + m[4] * ndc.y + m[5] * ndc.z,
@@ -579,22 +577,28 @@ struct EdgeGeom {
     double dist, pdf;
 };
 
-// pmf.h:103-167 sampleReuse on a normalised CDF with a leading 0 (n+1 entries)
+// pmf.h:103-167 sampleReuse on a normalised CDF with a leading 0 (n+1 entries). The CDF
+// entries and u are non-negative doubles, whose IEEE bit patterns order as 64-bit integers:
+// the search compares those on the integer pipe and leaves the FP64 pipe (1/64 of FP32 on
+// this GPU) to the reuse of u.
 DT_D int sample_reuse(const double *cdf, int n, double &u, double &pdf) {
+    const long long ub = __double_as_longlong(u);
     int lo = 0, hi = n + 1;  // lower_bound
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
-        if (cdf[mid] < u) lo = mid + 1;
+        if (__double_as_longlong(__ldg(cdf + mid)) < ub) lo = mid + 1;
         else hi = mid;
     }
     int idx = min(n - 1, max(0, lo - 1));
-    while (cdf[idx + 1] - cdf[idx] == 0.0 && idx < n - 1) ++idx;
-    pdf = cdf[idx + 1] - cdf[idx];
-    u = (u - cdf[idx]) / pdf;
+    while (idx < n - 1 && __double_as_longlong(__ldg(cdf + idx + 1)) == __double_as_longlong(__ldg(cdf + idx))) ++idx;
+    const double c0 = __ldg(cdf + idx);
+    pdf = __ldg(cdf + idx + 1) - c0;
+    u = (u - c0) / pdf;
     return idx;
 }
 
-// shape.cpp:302-335
+// shape.cpp:302-335, in FP64. The side of each face plane is the sign of the dot product
+// with the face's unnormalised normal (normalising by a positive length keeps the sign).
 DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) {
     if (e.f0 < 0 || e.f1 < 0) return 2;
     const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
@@ -605,7 +609,7 @@ DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) 
         for (int i = 0; i < 3; ++i) {
             if (ids[i] != e.v0 && ids[i] != e.v1) {
                 const double3_ v = tod(f3(__ldg(sc.verts + ids[i])));
-                const double3_ n = k == 0 ? normalized(crossd(v0 - v, v1 - v)) : normalized(crossd(v1 - v, v0 - v));
+                const double3_ n = k == 0 ? crossd(v0 - v, v1 - v) : crossd(v1 - v, v0 - v);
                 ff[k] = dotd(n, p - v) > 0.0;
                 break;
             }
@@ -615,44 +619,75 @@ DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) 
     return sc.shapes[e.shape].has_normals ? 0 : 1;
 }
 
-// volpathAD.cpp:231-280 / 540-589 (ALTERNATIVE_EDGE_SAMPLING): the angularly interpolated
-// direction to the edge point, its derivative slots and the angular pdf, all in FP64.
-template <int N>
-DT_D bool edge_direction(const DevScene &sc, const DevEdge &e, const double3_ &x0, const double (*x0d)[3], double t,
-                         double &pdf, double3_ &w1, double (*w1d)[3], double &dist, double3_ &nrm) {
+// volpathAD.cpp:231-280 / 540-589 (ALTERNATIVE_EDGE_SAMPLING): the edge point seen from x0
+// at parameter t, by angular interpolation between the edge's endpoints, in FP64 (near-
+// degenerate triangles cancel). w0 : wb = sin(theta (1 - t)) / l0 : sin(theta t) / l1,
+// normalised to a sum of 1; pdf is divided by theta.
+struct EdgePoint {
+    double3_ w1, nrm;   // unit direction to the edge point, unit normal of (x0, v0, v1)
+    double dist, w0, wb;
+};
+DT_D bool edge_point_solve(const DevScene &sc, const DevEdge &e, const double3_ &x0, double t, double &pdf,
+                           EdgePoint &ep) {
     const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
     const double3_ e0 = v0 - x0, e1 = v1 - x0;
-    nrm = normalized(crossd(e0, e1));
+    ep.nrm = normalized(crossd(e0, e1));
     const double l0 = lengthd(e0), l1 = lengthd(e1);
     const double c = fmin(1.0, fmax(-1.0, dotd(e0, e1) / (l0 * l1)));
-    const double theta = acos(c), st = sin(theta);
+    const double theta = acos(c);
     if (theta < kEpsD || theta > kPiD - kEpsD) return false;
-    double w0 = sin(theta * (1.0 - t)) / st / l0, wb = sin(theta * t) / st / l1;
-    const double tmp = w0 + wb;
-    w0 /= tmp;
-    wb /= tmp;
+    // the common factor 1 / sin(theta) of both weights cancels in the normalisation
+    double w0 = sin(theta * (1.0 - t)) * l1, wb = sin(theta * t) * l0;
+    const double inv = 1.0 / (w0 + wb);
+    w0 *= inv;
+    wb *= inv;
     if (w0 < -kEpsD || wb < -kEpsD || fabs(w0 + wb - 1.0) > kEpsD) return false;
     const double3_ w = e0 * w0 + e1 * wb;
-    dist = lengthd(w);
-    w1 = w * (1.0 / dist);
-    double mx = 0.0;
+    ep.dist = lengthd(w);
+    ep.w1 = w * (1.0 / ep.dist);
+    ep.w0 = w0;
+    ep.wb = wb;
+    pdf /= theta;
+    return true;
+}
+
+// Derivative slots of the edge-point direction (FP32: they are stored as FP32 weights):
+// dw = w0 (dv0 - dx0) + wb (dv1 - dx0), dw1 = (dw - w1 (w1 . dw)) / dist, and the slot
+// weight s_j = (n . dw1_j) k2. False where no slot moves the direction (every component at
+// most 1e-7) or where dw1 leaves the plane normal to w1 by more than 1e-7: w1 . dw1 =
+// (w1 . dw)(1 - |w1|^2) / dist, with |w1|^2 from the FP64 solve.
+template <int N>
+DT_D bool edge_point_slots(const DevScene &sc, const DevEdge &e, const EdgePoint &ep, const float (*x0d)[3], double k2,
+                           float *s) {
+    const float3 w1 = tof(ep.w1), nrm = tof(ep.nrm);
+    const float w0 = (float)ep.w0, wb = (float)ep.wb, inv_d = (float)(1.0 / ep.dist), k2f = (float)k2;
+    const float off_plane = (float)fabs(1.0 - dotd(ep.w1, ep.w1)) * inv_d;
+    float mx = 0.f;
+    bool moves = false;
+#pragma unroll
     for (int j = 0; j < N; ++j) {
-        double dv0[3] = {0, 0, 0}, dv1[3] = {0, 0, 0};
+        float3 dv0 = mk(0.f, 0.f, 0.f), dv1 = dv0;
         if (sc.vert_der) {
             const float *g0 = sc.vert_der + (size_t)e.v0 * sc.nder * 3 + 3 * j;
             const float *g1 = sc.vert_der + (size_t)e.v1 * sc.nder * 3 + 3 * j;
-            for (int k = 0; k < 3; ++k) { dv0[k] = g0[k]; dv1[k] = g1[k]; }
+            dv0 = mk(g0[0], g0[1], g0[2]);
+            dv1 = mk(g1[0], g1[1], g1[2]);
         }
-        double dw[3];
-        for (int k = 0; k < 3; ++k) dw[k] = (dv0[k] - x0d[j][k]) * w0 + (dv1[k] - x0d[j][k]) * wb;
-        const double proj = w1.x * dw[0] + w1.y * dw[1] + w1.z * dw[2];
-        w1d[j][0] = (dw[0] - w1.x * proj) / dist;
-        w1d[j][1] = (dw[1] - w1.y * proj) / dist;
-        w1d[j][2] = (dw[2] - w1.z * proj) / dist;
-        mx = fmax(mx, fabs(w1d[j][0] * w1.x + w1d[j][1] * w1.y + w1d[j][2] * w1.z));
+        const float3 xd = mk(x0d[j][0], x0d[j][1], x0d[j][2]);
+        const float3 dw = (dv0 - xd) * w0 + (dv1 - xd) * wb;
+        const float proj = dot(w1, dw);
+        const float3 d1 = (dw - w1 * proj) * inv_d;
+        mx = fmaxf(mx, fabsf(proj) * off_plane);
+        moves = moves || fabsf(d1.x) > (float)kEpsD || fabsf(d1.y) > (float)kEpsD || fabsf(d1.z) > (float)kEpsD;
+        s[j] = dot(nrm, d1) * k2f;
     }
-    pdf /= theta;
-    return !(mx > kEpsD);
+    return moves && !(mx > (float)kEpsD);
+}
+
+// The two sub-path directions of an edge sample, w1 -+ kAngleEps n (volpathAD.cpp:601-605)
+DT_D float3 edge_subpath_dir(const EdgePoint &ep, int sgn) {
+    const float a = sgn == 0 ? -kAngleEps : kAngleEps;
+    return normalize(tof(ep.w1) + tof(ep.nrm) * a);
 }
 
 template <int N>
@@ -680,22 +715,13 @@ __global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Q
         const DevEdge e = sc.edges[shp.edge_off + (has ? k : 0)];
         const double3_ x0 = mkd(r.x0[0], r.x0[1], r.x0[2]);
         bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL && is_silhouette(sc, e, x0) > 0;
-        double x0d[N][3];
-#pragma unroll
-        for (int j = 0; j < N; ++j)
-            for (int q = 0; q < 3; ++q) x0d[j][q] = r.x0d[j][q];
-        double3_ w1, nrm;
-        double w1d[N][3], dist;
-        if (ok) ok = edge_direction<N>(sc, e, x0, x0d, u, pdf, w1, w1d, dist, nrm);
-        if (ok) {
-            bool dz = true;
-            for (int j = 0; j < N; ++j)
-                for (int q = 0; q < 3; ++q) dz = dz && fabs(w1d[j][q]) <= kEpsD;
-            ok = !dz;
-        }
+        EdgePoint ep;
+        float s[N];
+        if (ok) ok = edge_point_solve(sc, e, x0, u, pdf, ep);
+        if (ok) ok = edge_point_slots<N>(sc, e, ep, r.x0d, 1.0 / (pdf * rp.sppse), s);
         float3 val = mk(0.f, 0.f, 0.f);
         int med1 = r.med;
-        const float3 w1f = tof(w1);
+        const float3 w1f = ok ? tof(ep.w1) : mk(0.f, 0.f, 1.f);
         if (ok) {
             if (r.kind == 0) {
                 Frame fr;
@@ -709,23 +735,19 @@ __global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Q
             ok = !is_zero3(val);
         }
         if (ok) {
-            const float tr = eval_transmittance(sc, stack, tof(x0), w1f, r.kind == 0, med1, (float)dist, rng, r.depth, c);
+            const float tr =
+                eval_transmittance(sc, stack, tof(x0), w1f, r.kind == 0, med1, (float)ep.dist, rng, r.depth, c);
             ok = tr > kEps;
         }
         if (ok) {
-            float s[N];
-            const double k2 = 1.0 / (pdf * rp.sppse);
-#pragma unroll
-            for (int j = 0; j < N; ++j) s[j] = (float)((nrm.x * w1d[j][0] + nrm.y * w1d[j][1] + nrm.z * w1d[j][2]) * k2);
             // the two sub-paths of a sample in adjacent slots: k_li then traces the nearly
             // identical rays (1e-4 rad apart) in neighbouring lanes of one warp
             const long long slot = queue_reserve_n(sc, qli, 2);
             for (int sgn = 0; sgn < 2 && slot >= 0; ++sgn) {
-                const double a = sgn == 0 ? -(double)kAngleEps : (double)kAngleEps;
-                const double3_ w2 = normalized(w1 + nrm * a);
+                const float3 w2 = edge_subpath_dir(ep, sgn);
                 LiTask<N> &t = reinterpret_cast<LiTask<N> *>(qli.data)[slot + sgn];
-                t.o[0] = (float)x0.x; t.o[1] = (float)x0.y; t.o[2] = (float)x0.z;
-                t.d[0] = (float)w2.x; t.d[1] = (float)w2.y; t.d[2] = (float)w2.z;
+                t.o[0] = r.x0[0]; t.o[1] = r.x0[1]; t.o[2] = r.x0[2];
+                t.d[0] = w2.x; t.d[1] = w2.y; t.d[2] = w2.z;
                 const float sg = sgn == 0 ? 1.f : -1.f;
                 t.w[0] = val.x * sg; t.w[1] = val.y * sg; t.w[2] = val.z * sg;
 #pragma unroll
@@ -739,8 +761,10 @@ __global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Q
 }
 
 // ====================================================================== Li sub-paths
+// Six resident blocks per SM (80 registers, a few spilled): traversal is latency bound and
+// the extra warps hide more of it than the spills cost (C2 Li stage 121 -> 102 ms).
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_li(DevScene sc, RenderParams rp, Queue qli, long long begin, long long count,
+__global__ void __launch_bounds__(kBlock, 6) k_li(DevScene sc, RenderParams rp, Queue qli, long long begin, long long count,
                                                double *acc1, double *acc2, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
@@ -878,12 +902,31 @@ __global__ void __launch_bounds__(kBlock) k_lins(DevScene sc, RenderParams rp, Q
 }
 
 // ====================================================================== primary edges
-// compute_intersection_in_tri, utils.cpp:256-266
-DT_D double intersection_in_tri(const double *b0, const double *c0, const double *b1, const double *c1, double t0) {
-    auto nrm = [](const double *a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); };
-    const double cb = nrm(b0) / nrm(b1), cc = nrm(c0) / nrm(c1);
-    const double bx = (1.0 - t0) * cb, by = t0 * cc;
-    return by / (bx + by);
+// A primary-edge sample's point (edge_manager.cpp:112-134, camera.cpp): the screen point at
+// parameter u along the edge, its pixel, the edge's unit screen normal, and the distance to
+// the edge point in camera space (the edge-point solve of compute_intersection_in_tri,
+// utils.cpp:256-266, with the edge's constants precomputed on the host), in FP64.
+struct PrimaryPoint {
+    double px, py, nx, ny;
+    int ipx, ipy;
+    float maxd;
+};
+DT_D void primary_edge_point(const DevCamera &cam, const DevPrimaryEdge &e, double u, PrimaryPoint &pp) {
+    pp.px = e.v0s[0] + (e.v1s[0] - e.v0s[0]) * u;
+    pp.py = e.v0s[1] + (e.v1s[1] - e.v0s[1]) * u;
+    pp.ipx = (int)floor(pp.px);
+    pp.ipy = (int)floor(pp.py);
+    pp.nx = e.n[0];
+    pp.ny = e.n[1];
+    const double a0 = (pp.px * cam.inv_w - 0.5) * cam.plane_kx - e.v0p[0];
+    const double a1 = (pp.py * cam.inv_h - 0.5) * cam.plane_ky - e.v0p[1];
+    const double a2 = 1.0 - e.v0p[2];
+    const double t0 = sqrt(a0 * a0 + a1 * a1 + a2 * a2) * e.inv_lenp;
+    const double bx = (1.0 - t0) * e.cb, by = t0 * e.cc;
+    const double t1 = by / (bx + by);
+    double pc[3];
+    for (int q = 0; q < 3; ++q) pc[q] = e.v0c[q] + t1 * (e.v1c[q] - e.v0c[q]);
+    pp.maxd = (float)sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
 }
 
 template <int N>
@@ -898,35 +941,26 @@ __global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp
         Rng rng;
         rng.init(rp.seed, child_key(0x5052494DULL, (uint32_t)(k >> 32), (uint32_t)k));
         n = 1;
-        // edge_manager.cpp:112-134
         double u = rng.next1d(), pdf;
         const int idx = sample_reuse(sc.pedge_cdf, sc.num_pedges, u, pdf);
         const DevPrimaryEdge &e = sc.pedges[idx];
         const DevCamera &cam = sc.cam;
-        double px_ = e.v0s[0] + (e.v1s[0] - e.v0s[0]) * u, py_ = e.v0s[1] + (e.v1s[1] - e.v0s[1]) * u;
-        float pdx[N], pdy[N];
+        PrimaryPoint pp;
+        primary_edge_point(cam, e, u, pp);
+        // screen velocity of the edge point along its normal, per slot (FP32)
+        const float uf = (float)u, nxf = (float)pp.nx, nyf = (float)pp.ny;
+        float sv[N];
         bool moving = false;
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            pdx[j] = (float)(e.d0[j][0] + (e.d1[j][0] - e.d0[j][0]) * u);
-            pdy[j] = (float)(e.d0[j][1] + (e.d1[j][1] - e.d0[j][1]) * u);
-            moving = moving || fabsf(pdx[j]) > kEps || fabsf(pdy[j]) > kEps;
+            const float pdx = e.d0[j][0] + (e.d1[j][0] - e.d0[j][0]) * uf;
+            const float pdy = e.d0[j][1] + (e.d1[j][1] - e.d0[j][1]) * uf;
+            moving = moving || fabsf(pdx) > kEps || fabsf(pdy) > kEps;
+            sv[j] = nxf * pdx + nyf * pdy;
         }
-        const double fov = cam.fov, aspect = (double)cam.width / cam.height;
-        const double tmp[3] = {(px_ / cam.width - 0.5) * 2.0 / fov, (py_ / cam.height - 0.5) * (-2.0) / (aspect * fov), 1.0};
-        const int ipx = (int)floor(px_), ipy = (int)floor(py_);
-        double nx = e.v1s[1] - e.v0s[1], ny = e.v0s[0] - e.v1s[0];
-        const double nl = sqrt(nx * nx + ny * ny);
-        nx /= nl;
-        ny /= nl;
-        const double fx = px_ - ipx, fy = py_ - ipy;
-        double a[3], bb[3];
-        for (int q = 0; q < 3; ++q) { a[q] = tmp[q] - e.v0p[q]; bb[q] = e.v1p[q] - e.v0p[q]; }
-        const double t0 = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) / sqrt(bb[0] * bb[0] + bb[1] * bb[1] + bb[2] * bb[2]);
-        const double t1 = intersection_in_tri(e.v0p, e.v1p, e.v0c, e.v1c, t0);
-        double pc[3];
-        for (int q = 0; q < 3; ++q) pc[q] = e.v0c[q] + t1 * (e.v1c[q] - e.v0c[q]);
-        const float maxd = (float)sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+        const int ipx = pp.ipx, ipy = pp.ipy;
+        const double fx = pp.px - ipx, fy = pp.py - ipy, nx = pp.nx, ny = pp.ny;
+        const float maxd = pp.maxd;
         const int lx = ipx - rp.crop_x, ly = ipy - rp.crop_y;
         if (moving && lx >= 0 && ly >= 0 && lx < rp.out_w && ly < rp.out_h) {
             float3 o, d;
@@ -944,7 +978,7 @@ __global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp
                     const float w = (float)(sgn == 0 ? rp.prim_weight : -rp.prim_weight);
                     t.w[0] = w; t.w[1] = w; t.w[2] = w;
 #pragma unroll
-                    for (int j = 0; j < N; ++j) t.s[j] = (float)(nx * pdx[j] + ny * pdy[j]);
+                    for (int j = 0; j < N; ++j) t.s[j] = sv[j];
                     t.med = cam.med_id; t.depth = rp.max_bounces; t.pixel = lx + rp.out_w * ly; t.flags = 1 | 2;
                     t.key = child_key(0x50524D31ULL + (uint64_t)k, 9u + (uint32_t)sgn, 0u);
                 }

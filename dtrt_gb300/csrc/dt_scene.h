@@ -92,6 +92,11 @@ struct DevCamera {
     float ndc2cam[9];
     float cpos[3], cframe[3][3];              // frame rows: s, t, n
     float d_cpos[kMaxNder][3], d_cframe[kMaxNder][3][3];
+    // reciprocals of the divisions on every camera ray and primary-edge sample (the FP64
+    // pipe runs at 1/64 of FP32: one division is about ten of its instructions)
+    double inv_w, inv_h;     // 1 / width, 1 / height
+    double ndc_ky;           // -2 / aspect
+    double plane_kx, plane_ky;  // 2 / fov, -2 / (aspect fov): pixel to image plane
 };
 
 struct DevEdge {
@@ -104,6 +109,9 @@ struct DevPrimaryEdge {
     double v0s[2], v1s[2];               // screen position in pixels
     float d0[kMaxNder][2], d1[kMaxNder][2];
     double v0p[3], v1p[3], v0c[3], v1c[3]; // image plane and camera-space endpoints
+    // per-edge constants of the edge-point solve (utils.cpp:256-266): unit screen-space
+    // normal, 1 / |v1p - v0p|, |v0p| / |v0c| and |v1p| / |v1c|
+    double n[2], inv_lenp, cb, cc;
 };
 
 struct __align__(16) BvhNode {

@@ -332,32 +332,11 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
         const DevEdge e = sc.edges[shp.edge_off + (has ? k : 0)];
         const double3_ x0 = mkd(r.x0[0], r.x0[1], r.x0[2]);
         bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL && is_silhouette(sc, e, x0) > 0;
-        // edge_direction with no derivative slots: direction, pdf and interpolation weights
-        double3_ w1, nrm;
-        double dist = 0.0, w0 = 0.0, wb = 0.0;
-        if (ok) {
-            const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
-            const double3_ e0 = v0 - x0, e1 = v1 - x0;
-            nrm = normalized(crossd(e0, e1));
-            const double l0 = lengthd(e0), l1 = lengthd(e1);
-            const double cth = fmin(1.0, fmax(-1.0, dotd(e0, e1) / (l0 * l1)));
-            const double theta = acos(cth), st = sin(theta);
-            ok = !(theta < kEpsD || theta > kPiD - kEpsD);
-            if (ok) {
-                w0 = sin(theta * (1.0 - u)) / st / l0;
-                wb = sin(theta * u) / st / l1;
-                const double tmp = w0 + wb;
-                w0 /= tmp;
-                wb /= tmp;
-                ok = !(w0 < -kEpsD || wb < -kEpsD || fabs(w0 + wb - 1.0) > kEpsD);
-            }
-            if (ok) {
-                const double3_ w = e0 * w0 + e1 * wb;
-                dist = lengthd(w);
-                w1 = w * (1.0 / dist);
-                pdf /= theta;
-            }
-        }
+        // the edge-point solve of k_edge: direction, pdf and interpolation weights
+        EdgePoint ep;
+        if (ok) ok = edge_point_solve(sc, e, x0, u, pdf, ep);
+        const double3_ w1 = ok ? ep.w1 : mkd(0.0, 0.0, 1.0), nrm = ok ? ep.nrm : mkd(0.0, 0.0, 1.0);
+        const double dist = ok ? ep.dist : 0.0, w0 = ok ? ep.w0 : 0.0, wb = ok ? ep.wb : 0.0;
         float3 val = mk(0.f, 0.f, 0.f);
         int med1 = -1;
         const float3 w1f = ok ? tof(w1) : mk(0.f, 0.f, 1.f);
@@ -379,11 +358,10 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
             const float3 c0 = tof(m * w0), c1 = tof(m * wb), cx = tof(m * (-(w0 + wb)));
             const long long slot = queue_reserve_n(sc, qli, 2);  // the pair in adjacent slots
             for (int sgn = 0; sgn < 2 && slot >= 0; ++sgn) {
-                const double a = sgn == 0 ? -(double)kAngleEps : (double)kAngleEps;
-                const double3_ w2 = normalized(w1 + nrm * a);
+                const float3 w2 = edge_subpath_dir(ep, sgn);
                 VLiTask &t = reinterpret_cast<VLiTask *>(qli.data)[slot + sgn];
-                t.o[0] = (float)x0.x; t.o[1] = (float)x0.y; t.o[2] = (float)x0.z;
-                t.d[0] = (float)w2.x; t.d[1] = (float)w2.y; t.d[2] = (float)w2.z;
+                t.o[0] = r.x0[0]; t.o[1] = r.x0[1]; t.o[2] = r.x0[2];
+                t.d[0] = w2.x; t.d[1] = w2.y; t.d[2] = w2.z;
                 const float sg = sgn == 0 ? 1.f : -1.f;
                 t.w[0] = val.x * sg; t.w[1] = val.y * sg; t.w[2] = val.z * sg;
                 t.c0[0] = c0.x; t.c0[1] = c0.y; t.c0[2] = c0.z;
@@ -415,22 +393,11 @@ __global__ void __launch_bounds__(kBlock) k_vadj_primary(DevScene sc, RenderPara
         const int idx = sample_reuse(sc.pedge_cdf, sc.num_pedges, u, pdf);
         const DevPrimaryEdge &e = sc.pedges[idx];
         const DevCamera &cam = sc.cam;
-        const double px_ = e.v0s[0] + (e.v1s[0] - e.v0s[0]) * u, py_ = e.v0s[1] + (e.v1s[1] - e.v0s[1]) * u;
-        const double fov = cam.fov, aspect = (double)cam.width / cam.height;
-        const double tmp[3] = {(px_ / cam.width - 0.5) * 2.0 / fov, (py_ / cam.height - 0.5) * (-2.0) / (aspect * fov), 1.0};
-        const int ipx = (int)floor(px_), ipy = (int)floor(py_);
-        double nx = e.v1s[1] - e.v0s[1], ny = e.v0s[0] - e.v1s[0];
-        const double nl = sqrt(nx * nx + ny * ny);
-        nx /= nl;
-        ny /= nl;
-        const double fx = px_ - ipx, fy = py_ - ipy;
-        double a[3], bb[3];
-        for (int q = 0; q < 3; ++q) { a[q] = tmp[q] - e.v0p[q]; bb[q] = e.v1p[q] - e.v0p[q]; }
-        const double t0 = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]) / sqrt(bb[0] * bb[0] + bb[1] * bb[1] + bb[2] * bb[2]);
-        const double t1 = intersection_in_tri(e.v0p, e.v1p, e.v0c, e.v1c, t0);
-        double pc[3];
-        for (int q = 0; q < 3; ++q) pc[q] = e.v0c[q] + t1 * (e.v1c[q] - e.v0c[q]);
-        const float maxd = (float)sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+        PrimaryPoint pp;
+        primary_edge_point(cam, e, u, pp);
+        const int ipx = pp.ipx, ipy = pp.ipy;
+        const double fx = pp.px - ipx, fy = pp.py - ipy, nx = pp.nx, ny = pp.ny;
+        const float maxd = pp.maxd;
         const int lx = ipx - rp.crop_x, ly = ipy - rp.crop_y;
         if (lx >= 0 && ly >= 0 && lx < rp.out_w && ly < rp.out_h) {
             // screen velocity of the edge point: ((1-u) J0 + u J1) [dv0; dv1], J in pixels

@@ -326,20 +326,25 @@ def rmse_summary(G, run_spp, g_ref, ref_spp):
     """Gradient error against a high-spp forward-mode reference g_ref (ref_spp samples per
     pixel; same estimator): the bias of the run mean and its standard error, and the spp at
     which the RMSE sqrt(|bias|^2 + tr Cov(run) * run_spp / spp) falls to 1% of |g_ref|
-    (variance term measured from the runs; the bias term taken as measured)."""
+    (variance term measured from the runs). |g_hat - g_ref|^2 holds the Monte Carlo noise
+    of both sides, tr Cov / runs + tr Cov run_spp / ref_spp in expectation; the bias term
+    of the spp estimate is the excess over that noise (0 when the difference is all noise)."""
     runs = G.shape[0]
     g_hat = G.mean(0)
     tr = float(G.var(0, ddof=1).sum())
     ref2 = float(g_ref @ g_ref)
     b = g_hat - g_ref
     bias2 = float(b @ b)
-    se_bias = float(np.sqrt(tr / runs + tr * run_spp / ref_spp))  # noise of the run mean and of the reference
+    noise2 = tr / runs + tr * run_spp / ref_spp  # expected |g_hat - g_ref|^2 of an unbiased estimator
+    bias2_excess = max(0.0, bias2 - noise2)
     target2 = 1e-4 * ref2
     spp_var_only = run_spp * tr / target2
-    spp_with_bias = run_spp * tr / (target2 - bias2) if bias2 < target2 else float("inf")
-    return {"reference": f"forward mode at {ref_spp} spp", "rel_bias": float(np.sqrt(bias2 / ref2)),
-            "rel_bias_se": float(se_bias / np.sqrt(ref2)), "spp_to_1pct_variance_only": spp_var_only,
-            "spp_to_1pct_with_bias": spp_with_bias}
+    spp_with_bias = run_spp * tr / (target2 - bias2_excess) if bias2_excess < target2 else float("inf")
+    return {"reference": f"forward mode at {ref_spp} spp", "rel_diff": float(np.sqrt(bias2 / ref2)),
+            "rel_noise_expected": float(np.sqrt(noise2 / ref2)),
+            "rel_bias_excess": float(np.sqrt(bias2_excess / ref2)),
+            "diff_over_noise": float(bias2 / noise2) if noise2 > 0 else None,
+            "spp_to_1pct_variance_only": spp_var_only, "spp_to_1pct_with_bias": spp_with_bias}
 
 
 def grad_rmse_c3(size=None, runs=16, run_spp=64, ladder_max=64, seed=31, ref_spp=2048, full_passes=4):

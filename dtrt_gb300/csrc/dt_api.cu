@@ -1062,7 +1062,7 @@ int set_edge_weights(dtrt_scene *s, const float *w) {
 
 void free_scratch(Scratch &b) {
     void *ptrs[] = {b.acc1,     b.acc2,     b.out,     b.qe,     b.ql,      b.qli,       b.counts,   b.err,
-                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt};
+                    b.adj_dimg, b.adj_grad, b.adj_out, b.adj_img, b.cam_state, b.cam_q, b.cam_cnt, b.li_sort};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     b = Scratch();
@@ -1070,7 +1070,7 @@ void free_scratch(Scratch &b) {
 
 size_t scratch_bytes(const Scratch &b) {
     return b.acc1_n + b.acc2_n + b.out_n + b.qe_bytes + b.ql_bytes + b.qli_bytes + b.adj_dimg_n + b.adj_grad_n +
-           b.adj_out_n + b.adj_img_n + b.cam_state_bytes + b.cam_q_bytes + b.cam_cnt_bytes;
+           b.adj_out_n + b.adj_img_n + b.cam_state_bytes + b.cam_q_bytes + b.cam_cnt_bytes + b.li_sort_bytes;
 }
 
 // Render work buffers (queues of 16-24 Mi records, path states, accumulators: GBs) of the

@@ -414,4 +414,20 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
     return 0;
 }
 
+size_t radix_hist_entries(long long n) { return (size_t)kDigits * (size_t)((n + kTile - 1) / kTile); }
+
+int *radix_sort_bits(unsigned *keys, int *vals, unsigned *keys2, int *vals2, unsigned *hist, int n, int bits,
+                     cudaStream_t st) {
+    if (n <= 1) return vals;
+    const unsigned nblk = (unsigned)((n + kTile - 1) / kTile);
+    for (int shift = 0; shift < bits; shift += 4) {
+        k_radix_hist<<<nblk, kSortThreads, 0, st>>>(keys, n, shift, hist);
+        k_scan_excl<<<1, kScanThreads, 0, st>>>(hist, kDigits * (int)nblk, nullptr);
+        k_radix_scatter<<<nblk, kSortThreads, 0, st>>>(keys, vals, n, shift, hist, keys2, vals2);
+        std::swap(keys, keys2);
+        std::swap(vals, vals2);
+    }
+    return vals;
+}
+
 }  // namespace dt

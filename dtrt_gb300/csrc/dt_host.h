@@ -28,8 +28,38 @@ struct Scratch {
     // wavefront schedules: path states and vertex inputs, four path-index queues, per-level counts
     void *cam_state = nullptr, *cam_q = nullptr, *cam_cnt = nullptr;
     size_t cam_state_bytes = 0, cam_q_bytes = 0, cam_cnt_bytes = 0;
+    // sort of the Li sub-path pairs: keys, values, their double buffers and digit counts
+    void *li_sort = nullptr;
+    size_t li_sort_bytes = 0;
 
 };
+
+bool ensure_buffer(void **ptr, size_t *have, size_t need);
+
+// Buffers of the Li pair sort for queues of li_cap tasks (li_cap / 2 pairs): false (and
+// the allocation error cleared) when the device has no room, the Li kernels then read the
+// queue in order.
+inline bool ensure_li_sort(Scratch &sb, uint64_t li_cap) {
+    const long long cap = (long long)(li_cap / 2);
+    if (ensure_buffer(&sb.li_sort, &sb.li_sort_bytes, (size_t)cap * 16 + radix_hist_entries(cap) * 4)) return true;
+    cudaGetLastError();
+    return false;
+}
+
+// The n queued Li tasks' pairs (slots 2m, 2m + 1) in key order (k_li_keys) on stream st;
+// nullptr when n is odd or holds one pair (the queue is then read in order).
+template <class Task>
+const int *sort_li_pairs(const DevScene &sc, const Task *tasks, long long n, Scratch &sb, uint64_t li_cap,
+                         cudaStream_t st) {
+    const long long np = n / 2, cap = (long long)(li_cap / 2);
+    if ((n & 1) || np < 2 || np > cap) return nullptr;
+    unsigned *keys = (unsigned *)sb.li_sort, *keys2 = keys + cap;
+    int *vals = (int *)(keys2 + cap), *vals2 = vals + cap;
+    unsigned *hist = (unsigned *)(vals2 + cap);
+    k_li_keys<Task><<<(unsigned)((np + 255) / 256), 256, 0, st>>>(sc, tasks, np, keys, vals);
+    return radix_sort_bits(keys, vals, keys2, vals2, hist, (int)np, kLiSortKeyBits, st);
+}
+
 
 // Connectivity kept from the last build, so that a rebuild from a description with the
 // same triangles (an optimisation step that moves vertices) skips the edge search and
@@ -74,7 +104,6 @@ struct dtrt_scene {
 namespace dt {
 template <int N>
 int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on_device, cudaStream_t stream);
-bool ensure_buffer(void **ptr, size_t *have, size_t need);
 int render_adjoint(dtrt_scene *s, const dtrt_render_options *o, const float *d_image, float *image, float *d_density,
                    int on_device, cudaStream_t stream);
 cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const float *dimg, float *grad, double *img_acc,

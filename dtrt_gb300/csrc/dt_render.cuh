@@ -109,13 +109,20 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     uint64_t state_traffic = 0;  // wavefront path-state bytes read + written (counted when counters are on)
     bool used_wavefront = false;
     int rc = DTRT_OK;
+    // Li sub-path pairs sorted by origin and direction before k_li (needs a tree)
+    const bool li_sorted = sc.num_nodes > 0 && ensure_li_sort(sb, li_cap);
     // Li tasks are drained chunk by chunk so that the queue never exceeds li_cap
     auto drain_li = [&]() -> int {
         if ((rc = read_counts())) return rc;
         const unsigned long long n = std::min<unsigned long long>(hcnt[2], li_cap);
         tot_li += n;
         if (n)
-            if ((rc = timed(ms_li, [&] { k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, sb.acc1, sb.acc2, ctr); })))
+            if ((rc = timed(ms_li, [&] {
+                     const int *perm = li_sorted ? sort_li_pairs(sc, (const LiTask<N> *)qli.data, (long long)n, sb,
+                                                                 li_cap, st)
+                                                 : nullptr;
+                     k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, sb.acc1, sb.acc2, perm, ctr);
+                 })))
                 return rc;
         DT_CK(cudaMemsetAsync(sb.counts + 2, 0, sizeof(unsigned long long), st));
         return DTRT_OK;
@@ -389,7 +396,7 @@ int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, in
         const unsigned long long n = std::min<unsigned long long>(hcnt[2], kNoallocLiCap);
         tot_li += n;
         if (n) {
-            k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, acc1, acc2, nullptr);
+            k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, acc1, acc2, nullptr, nullptr);
             if ((rc = launched())) return rc;
         }
         DT_CK(cudaMemsetAsync(counts + 2, 0, sizeof(unsigned long long), st));

@@ -135,13 +135,17 @@ int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const flo
         DT_VCK(cudaStreamSynchronize(st));
         return DTRT_OK;
     };
+    const bool li_sorted = sc.num_nodes > 0 && ensure_li_sort(sb, li_cap);  // pairs by origin and direction
     auto drain_li = [&]() -> int {
         int r = read_counts();
         if (r) return r;
         const unsigned long long n = std::min<unsigned long long>(hcnt[2], li_cap);
         tot_li += n;
         if (n) {
-            k_vadj_li<<<blocks((long long)n), kBlock, 0, st>>>(sc, rp, qli, (long long)n, dimg, grad, xadj, ctr);
+            const int *perm = li_sorted ? sort_li_pairs(sc, (const VLiTask *)qli.data, (long long)n, sb, li_cap, st)
+                                        : nullptr;
+            k_vadj_li<<<blocks((long long)n), kBlock, 0, st>>>(sc, rp, qli, (long long)n, dimg, grad, xadj, perm,
+                                                               ctr);
             ++launches;
             DT_VCK(cudaGetLastError());
         }

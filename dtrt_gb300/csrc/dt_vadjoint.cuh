@@ -434,9 +434,10 @@ __global__ void __launch_bounds__(kBlock) k_vadj_primary(DevScene sc, RenderPara
     if (ctr) flush_counters(ctr, K_PRIMARY, c, CT_PRIMARY, n);
 }
 
-// one thread per VLiTask: Li, then K = dot(dL/dI, w (x) Li) times the coefficients
-__global__ void __launch_bounds__(kBlock) k_vadj_li(DevScene sc, RenderParams rp, Queue qli, long long count,
-                                                    const float *dimg, float *grad, float *xadj,
+// one thread per VLiTask: Li, then K = dot(dL/dI, w (x) Li) times the coefficients; six
+// resident blocks per SM and the pairs in sorted order (perm, or queue order), as k_li
+__global__ void __launch_bounds__(kBlock, 6) k_vadj_li(DevScene sc, RenderParams rp, Queue qli, long long count,
+                                                    const float *dimg, float *grad, float *xadj, const int *perm,
                                                     unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
@@ -444,7 +445,8 @@ __global__ void __launch_bounds__(kBlock) k_vadj_li(DevScene sc, RenderParams rp
     Ctr c;
     uint32_t n = 0;
     if (gi < count) {
-        const VLiTask &t = reinterpret_cast<const VLiTask *>(qli.data)[gi];
+        const long long slot = perm ? 2LL * __ldg(perm + (gi >> 1)) + (gi & 1) : gi;
+        const VLiTask &t = reinterpret_cast<const VLiTask *>(qli.data)[slot];
         Rng rng;
         rng.init(rp.seed, t.key);
         n = 1;

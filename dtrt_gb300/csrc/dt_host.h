@@ -60,6 +60,18 @@ const int *sort_li_pairs(const DevScene &sc, const Task *tasks, long long n, Scr
     return radix_sort_bits(keys, vals, keys2, vals2, hist, (int)np, kLiSortKeyBits, st);
 }
 
+// The primary-edge samples [rp.prim_begin, + rp.prim_count) in key order (k_primary_keys),
+// in the Li sort's buffers (a chunk holds at most li_cap / 2 samples); nullptr for one.
+inline const int *sort_primary_samples(const RenderParams &rp, Scratch &sb, uint64_t li_cap, cudaStream_t st) {
+    const long long cap = (long long)(li_cap / 2);
+    if (rp.prim_count < 2 || rp.prim_count > cap) return nullptr;
+    unsigned *keys = (unsigned *)sb.li_sort, *keys2 = keys + cap;
+    int *vals = (int *)(keys2 + cap), *vals2 = vals + cap;
+    unsigned *hist = (unsigned *)(vals2 + cap);
+    k_primary_keys<<<(unsigned)((rp.prim_count + 255) / 256), 256, 0, st>>>(rp, keys, vals);
+    return radix_sort_bits(keys, vals, keys2, vals2, hist, (int)rp.prim_count, 20, st);
+}
+
 
 // Connectivity kept from the last build, so that a rebuild from a description with the
 // same triangles (an optimisation step that moves vertices) skips the edge search and

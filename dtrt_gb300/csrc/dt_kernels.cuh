@@ -971,15 +971,31 @@ DT_D void primary_edge_point(const DevCamera &cam, const DevPrimaryEdge &e, doub
     pp.maxd = (float)sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
 }
 
+// Sort key of primary-edge sample k: the top 20 bits of its first random number, which
+// picks the edge and the point on it (sample_reuse): samples in key order lie along the
+// edge list, so a warp traces neighbouring camera rays (C2 primary-edge stage 26.4 ->
+// 16.3 ms with the sort). The sample's random numbers stay keyed by k.
+template <int Unused = 0>
+__global__ void k_primary_keys(RenderParams rp, unsigned *keys, int *vals) {
+    const long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= rp.prim_count) return;
+    const long long k = rp.prim_begin + gi;
+    Rng rng;
+    rng.init(rp.seed, child_key(0x5052494DULL, (uint32_t)(k >> 32), (uint32_t)k));
+    keys[gi] = rng.next_u32() >> 12;
+    vals[gi] = (int)gi;
+}
+
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp, Queue qli, unsigned long long *ctr) {
+__global__ void __launch_bounds__(kBlock) k_primary(DevScene sc, RenderParams rp, Queue qli, const int *perm,
+                                                    unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
     Ctr c;
     uint32_t n = 0;
     if (gi < rp.prim_count) {
-        const long long k = rp.prim_begin + gi;
+        const long long k = rp.prim_begin + (perm ? (long long)__ldg(perm + gi) : gi);
         Rng rng;
         rng.init(rp.seed, child_key(0x5052494DULL, (uint32_t)(k >> 32), (uint32_t)k));
         n = 1;

@@ -231,7 +231,8 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
             rp.prim_begin = k0;
             rp.prim_count = std::min(chunk, ns - k0);
             if ((rc = timed(ms_primary, [&] {
-                     k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, ctr);
+                     const int *perm = li_sorted ? sort_primary_samples(rp, sb, li_cap, st) : nullptr;
+                     k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, perm, ctr);
                  })))
                 return rc;
             if ((rc = drain_li())) return rc;
@@ -443,7 +444,7 @@ int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, in
         for (long long k0 = 0; k0 < ns; k0 += chunk) {
             rp.prim_begin = k0;
             rp.prim_count = std::min(chunk, ns - k0);
-            k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, nullptr);
+            k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, nullptr, nullptr);
             if ((rc = launched())) return rc;
             if ((rc = drain_li())) return rc;
         }

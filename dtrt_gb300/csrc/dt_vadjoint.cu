@@ -189,7 +189,8 @@ int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const flo
         for (long long k0 = 0; k0 < ns; k0 += chunk) {
             rp.prim_begin = k0;
             rp.prim_count = std::min(chunk, ns - k0);
-            k_vadj_primary<<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, ctr);
+            const int *perm = li_sorted ? sort_primary_samples(rp, sb, li_cap, st) : nullptr;
+            k_vadj_primary<<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, perm, ctr);
             ++launches;
             DT_VCK(cudaGetLastError());
             if ((rc = drain_li())) return rc;

@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
 }
 
 // one thread per primary-edge sample: k_primary's geometry with the projection Jacobian
-__global__ void __launch_bounds__(kBlock) k_vadj_primary(DevScene sc, RenderParams rp, Queue qli,
+__global__ void __launch_bounds__(kBlock) k_vadj_primary(DevScene sc, RenderParams rp, Queue qli, const int *perm,
                                                          unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(kBlock) k_vadj_primary(DevScene sc, RenderPara
     Ctr c;
     uint32_t n = 0;
     if (gi < rp.prim_count) {
-        const long long k = rp.prim_begin + gi;
+        const long long k = rp.prim_begin + (perm ? (long long)__ldg(perm + gi) : gi);  // sorted order, as k_primary
         Rng rng;
         rng.init(rp.seed, child_key(0x5052494DULL, (uint32_t)(k >> 32), (uint32_t)k));
         n = 1;

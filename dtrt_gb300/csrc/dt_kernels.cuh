@@ -684,6 +684,23 @@ DT_D bool edge_point_slots(const DevScene &sc, const DevEdge &e, const EdgePoint
     return moves && !(mx > (float)kEpsD);
 }
 
+// A reflection-only BSDF at x0 (diffuse.cpp:7-12, phong.cpp:19-53: zero unless wi.z and
+// wo.z >= 1e-7) gives an edge sample of a surface record a zero value when the incident
+// direction is below the shading plane, or when both edge endpoints lie below it by more
+// than 1e-4 of their distance: w1 is a non-negative combination of the directions to the
+// endpoints, so its cosine with the normal is then below -1e-4, far beyond FP32 rounding.
+// Such samples skip the FP64 silhouette test and edge-point solve; the value test after
+// them would reject them all the same (no random numbers are drawn in between).
+DT_D bool edge_sample_is_zero(const DevScene &sc, int shape, const float *wi, const float *fn, const float *x0,
+                              const DevEdge &e) {
+    const int t = sc.bsdfs[sc.shapes[shape].bsdf_id].type;
+    if (t != BSDF_DIFFUSE && t != BSDF_PHONG) return false;
+    if (wi[2] < kEps) return true;
+    const float3 n = mk(fn[0], fn[1], fn[2]), p = mk(x0[0], x0[1], x0[2]);
+    const float3 a = f3(__ldg(sc.verts + e.v0)) - p, b = f3(__ldg(sc.verts + e.v1)) - p;
+    return dot(a, n) < -1e-4f * length(a) && dot(b, n) < -1e-4f * length(b);
+}
+
 // The two sub-path directions of an edge sample, w1 -+ kAngleEps n (volpathAD.cpp:601-605)
 DT_D float3 edge_subpath_dir(const EdgePoint &ep, int sgn) {
     const float a = sgn == 0 ? -kAngleEps : kAngleEps;
@@ -714,7 +731,9 @@ __global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Q
         double pdf = has ? pdf_shape * pdf_edge : 0.0;
         const DevEdge e = sc.edges[shp.edge_off + (has ? k : 0)];
         const double3_ x0 = mkd(r.x0[0], r.x0[1], r.x0[2]);
-        bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL && is_silhouette(sc, e, x0) > 0;
+        bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL &&
+                  !(r.kind == 0 && edge_sample_is_zero(sc, r.shape, r.wi, r.fn, r.x0, e)) &&
+                  is_silhouette(sc, e, x0) > 0;
         EdgePoint ep;
         float s[N];
         if (ok) ok = edge_point_solve(sc, e, x0, u, pdf, ep);

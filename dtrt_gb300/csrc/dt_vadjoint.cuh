@@ -331,7 +331,8 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
         double pdf = has ? pdf_shape * pdf_edge : 0.0;
         const DevEdge e = sc.edges[shp.edge_off + (has ? k : 0)];
         const double3_ x0 = mkd(r.x0[0], r.x0[1], r.x0[2]);
-        bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL && is_silhouette(sc, e, x0) > 0;
+        bool ok = has && sc.bsdfs[shp.bsdf_id].type != BSDF_NULL &&
+                  !edge_sample_is_zero(sc, r.shape, r.wi, r.fn, r.x0, e) && is_silhouette(sc, e, x0) > 0;
         // the edge-point solve of k_edge: direction, pdf and interpolation weights
         EdgePoint ep;
         if (ok) ok = edge_point_solve(sc, e, x0, u, pdf, ep);

@@ -192,6 +192,50 @@ def choose_cpu_spp(oracle_py, spec, wl_name, target_s=4.0, nthreads=0):
 
 
 # --------------------------------------------------------------------------- GPU arm
+def roofline_of(wl_name, spec, cstats, kms, steps, paths_per_step, full_size=True):
+    """Roofline of the dominant kernel stage: algorithmic bytes per step (device counters of
+    one instrumented render: 64 B per BVH node visit, 48 B per triangle test, 32 B per
+    trilinear lookup, 8 B per light-CDF probe, and for the wavefront camera stage the path
+    state read and written per vertex launch) over the stage's CUDA-event time per step
+    (kms: stage -> ms summed over `steps` renders); traffic = DRAM bytes per path of an ncu
+    capture of that stage over one full render (profiles/traffic.json), scaled to the step."""
+    kernels = ["camera", "edge", "li", "lins", "primary"]
+    dom = max(kms, key=kms.get)
+    ki = kernels.index(dom)
+    node_b, tri_b, grid_b = 64, 48, 32
+    probe_b = 8 * light_cdf_probes(spec)  # one FP32/FP64 CDF entry per binary-search step
+    state_b = cstats["camera_state_bytes"] if dom == "camera" else 0
+    alg_terms = {"bvh_nodes": node_b * cstats["k_node_visits"][ki], "triangles": tri_b * cstats["k_tri_tests"][ki],
+                 "grid_lookups": grid_b * cstats["k_grid_lookups"][ki],
+                 "light_cdf_probes": probe_b * cstats["k_light_samples"][ki], "path_state": state_b}
+    alg_bytes = sum(alg_terms.values())
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (kms[dom] / steps / 1e3) / 1e9 if kms[dom] > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile) and full_size:
+        t = json.load(open(tfile)).get(f"{wl_name}:{dom}")
+        if t:
+            traffic = t["dram_bytes_per_path"] * paths_per_step
+    kname = f"k_{dom}"
+    if dom == "camera" and cstats.get("camera_schedule") == 2:
+        kname = ("k_cam_vertex (camera stage: k_cam_start, then per vertex level k_cam_vertex for the "
+                 "volume and the interface vertices, k_cam_accum)")
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": kname,
+            "peak_source": "measured" if peaks else "fallback",
+            "bytes_per_step": alg_bytes, "bytes_per_step_terms": alg_terms,
+            "traffic_over_algorithmic": traffic / alg_bytes if traffic and alg_bytes else None,
+            "bytes_model": "64 B per BVH node visit + 48 B per triangle test + 32 B per trilinear lookup + "
+                           "8 B per light-CDF probe (binary-search steps per emitter sample) + the wavefront "
+                           "path-state bytes read and written per vertex launch (CamState + VertexIn; device "
+                           "counters of one instrumented render)",
+            "traffic_note": "DRAM read+write per path of the stage's launches over one full render (ncu, "
+                            "profiles/traffic.json), scaled to the step's paths"}
+
+
 def run_gpu(args, wl_name, rank, world, local_rank):
     import torch
     from dtrt_gb300 import native
@@ -245,44 +289,9 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     e2e_dt = (time.perf_counter() - t0) / e2e_steps
     e2e = {"value": paths_per_step * world / e2e_dt, "unit": "paths/s", "h2d_bytes_per_step": spec_h2d_bytes(spec),
            "d2h_bytes_per_step": int(host_out.nbytes), "ms_per_step": e2e_dt * 1e3}
-    # roofline of the dominant kernel (per-launch algorithmic bytes / its event time)
-    kernels = ["camera", "edge", "li", "lins", "primary"]
     kms = {"camera": stage["ms_camera"], "edge": stage["ms_edge"], "li": stage["ms_li"],
            "primary": stage["ms_primary"]}
-    dom = max(kms, key=kms.get)
-    ki = kernels.index(dom)
-    node_b, tri_b, grid_b = 64, 48, 32
-    probe_b = 8 * light_cdf_probes(spec)  # one FP32/FP64 CDF entry per binary-search step
-    state_b = cstats["camera_state_bytes"] if dom == "camera" else 0
-    alg_terms = {"bvh_nodes": node_b * cstats["k_node_visits"][ki], "triangles": tri_b * cstats["k_tri_tests"][ki],
-                 "grid_lookups": grid_b * cstats["k_grid_lookups"][ki],
-                 "light_cdf_probes": probe_b * cstats["k_light_samples"][ki], "path_state": state_b}
-    alg_bytes = sum(alg_terms.values())
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    peak = peaks.get("hbm_gbs", 6800.0)
-    achieved = alg_bytes / (kms[dom] / args.steps / 1e3) / 1e9 if kms[dom] > 0 else 0.0
-    # DRAM bytes of the dominant kernel per step, from an ncu capture of one launch of it
-    # (per camera path, scaled to the step's paths; the capture's source is recorded)
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile) and args.size is None:
-        t = json.load(open(tfile)).get(f"{wl_name}:{dom}")
-        if t:
-            traffic = t["dram_bytes_per_path"] * paths_per_step
-    kname = f"k_{dom}"
-    if dom == "camera" and cstats.get("camera_schedule") == 2:
-        kname = ("k_cam_vertex (camera stage: k_cam_start, then per vertex level k_cam_vertex for the "
-                 "volume and the interface vertices, k_cam_accum)")
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if peak else None, "traffic": traffic, "kernel": kname,
-                "peak_source": "measured" if peaks else "fallback",
-                "bytes_per_step": alg_bytes, "bytes_per_step_terms": alg_terms,
-                "bytes_model": "64 B per BVH node visit + 48 B per triangle test + 32 B per trilinear lookup + "
-                               "8 B per light-CDF probe (binary-search steps per emitter sample) + the wavefront "
-                               "path-state bytes read and written per vertex launch (CamState + VertexIn; device "
-                               "counters of one instrumented render)",
-                "traffic_note": "dram read+write per step scaled from one ncu-captured launch (profiles/traffic.json)"}
+    roofline = roofline_of(wl_name, spec, cstats, kms, args.steps, paths_per_step, args.size is None)
     line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
@@ -798,7 +807,12 @@ def c3_forward(no_cpu=False, steps=3, warmup=1, cpu_target_s=4.0):
     out = torch.empty(spec.out_shape(), dtype=torch.float32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     paths = spec.width * spec.height * WORKLOADS["c3"]["spp"]
+    kms = {"camera": 0.0, "edge": 0.0, "li": 0.0, "primary": 0.0}
     with native.NativeScene(spec) as sc:
+        sc.enable_counters(True)  # instrumented render: the roofline's algorithmic bytes
+        sc.render(out.data_ptr(), stream=stream.cuda_stream, **kw(12345))
+        cstats = sc.last_stats()
+        sc.enable_counters(False)
         for k in range(warmup):
             sc.render(out.data_ptr(), stream=stream.cuda_stream, **kw(600 + k))
         ms = []
@@ -810,10 +824,14 @@ def c3_forward(no_cpu=False, steps=3, warmup=1, cpu_target_s=4.0):
             e1.record(stream)
             torch.cuda.synchronize()
             ms.append(e0.elapsed_time(e1))
+            st = sc.last_stats()
+            for key in kms:
+                kms[key] += st["ms_" + key]
     t = float(np.median(ms))
     res = {"workload": WORKLOADS["c3"]["desc"], "width": 512, "height": 512, "spp": WORKLOADS["c3"]["spp"],
            "max_bounces": 16, "nder": 8, "paths_per_s": paths / (t / 1e3), "ms_per_render": t,
-           "derivative_samples_per_s": paths * 8 / (t / 1e3)}
+           "derivative_samples_per_s": paths * 8 / (t / 1e3),
+           "roofline": roofline_of("c3", spec, cstats, kms, steps, paths)}
     if not no_cpu:
         cb = cpu_baseline("c3", cpu_target_s, runs=1)
         res["cpu_baseline"] = cb

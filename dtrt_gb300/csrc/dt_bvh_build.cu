@@ -131,9 +131,11 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned *key
     if (threadIdx.x < kDigits) hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = s_cnt[threadIdx.x];
 }
 
-// exclusive scan of m entries in one block (m is at most a few hundred thousand); *total = sum
+// exclusive scan of m entries per block (m is at most a few hundred thousand): block b scans
+// a[b m, (b + 1) m) and writes its sum to total[b] (when total is given)
 __global__ void __launch_bounds__(kScanThreads) k_scan_excl(unsigned *a, int m, unsigned *total) {
     __shared__ unsigned s[kScanThreads];
+    a += (size_t)blockIdx.x * m;
     const int per = (m + kScanThreads - 1) / kScanThreads;
     const int b0 = threadIdx.x * per, b1 = min(m, b0 + per);
     unsigned sum = 0;
@@ -152,11 +154,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_excl(unsigned *a, int m, 
         a[i] = run;
         run += v;
     }
-    if (threadIdx.x == kScanThreads - 1 && total) *total = s[kScanThreads - 1];
+    if (threadIdx.x == kScanThreads - 1 && total) total[blockIdx.x] = s[kScanThreads - 1];
 }
 
 // 3b. stable scatter of each tile by digit, rounds in element order, ranks within a warp
-// from __match_any_sync and across warps from per-warp digit counts
+// from __match_any_sync and across warps from per-warp digit counts. hist holds each
+// digit's row of block counts scanned within the row, then the kDigits row totals.
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned *keys, const int *vals, int n, int shift,
                                                                 const unsigned *hist, unsigned *keys_out,
                                                                 int *vals_out) {
@@ -164,7 +167,12 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned *
     __shared__ unsigned s_base[kDigits];
     __shared__ unsigned s_wcnt[kWarps][kDigits];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x < kDigits) s_base[threadIdx.x] = hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x];
+    if (threadIdx.x < kDigits) {
+        const unsigned *totals = hist + (size_t)kDigits * gridDim.x;
+        unsigned digit_base = 0;
+        for (int q = 0; q < (int)threadIdx.x; ++q) digit_base += totals[q];
+        s_base[threadIdx.x] = hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] + digit_base;
+    }
     const long long base = (long long)blockIdx.x * kTile;
     for (int r = 0; r < kSortRounds; ++r) {
         const long long i = base + (long long)r * kSortThreads + threadIdx.x;
@@ -347,7 +355,7 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
     unsigned *bounds = tmp.get<unsigned>(8);
     unsigned *keys = tmp.get<unsigned>(n), *keys2 = tmp.get<unsigned>(n);
     int *vals = tmp.get<int>(n), *vals2 = tmp.get<int>(n);
-    unsigned *hist = tmp.get<unsigned>((size_t)kDigits * nblk + 1);
+    unsigned *hist = tmp.get<unsigned>((size_t)kDigits * (nblk + 1));  // rows of block counts, row totals
     int *left = tmp.get<int>(m), *right = tmp.get<int>(m), *par_in = tmp.get<int>(m), *par_leaf = tmp.get<int>(n);
     int2 *range = tmp.get<int2>(m);
     float4 *leaf_box = tmp.get<float4>((size_t)2 * n), *node_box = tmp.get<float4>((size_t)2 * m);
@@ -370,7 +378,7 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
         for (int pass = 0; pass < 8; ++pass) {  // 32 key bits, 4 per pass
             const int shift = 4 * pass;
             k_radix_hist<<<nblk, kSortThreads, 0, st>>>(keys, n, shift, hist);
-            k_scan_excl<<<1, kScanThreads, 0, st>>>(hist, kDigits * nblk, nullptr);
+            k_scan_excl<<<kDigits, kScanThreads, 0, st>>>(hist, nblk, hist + (size_t)kDigits * nblk);
             k_radix_scatter<<<nblk, kSortThreads, 0, st>>>(keys, vals, n, shift, hist, keys2, vals2);
             std::swap(keys, keys2);
             std::swap(vals, vals2);
@@ -414,7 +422,7 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
     return 0;
 }
 
-size_t radix_hist_entries(long long n) { return (size_t)kDigits * (size_t)((n + kTile - 1) / kTile); }
+size_t radix_hist_entries(long long n) { return (size_t)kDigits * (size_t)((n + kTile - 1) / kTile + 1); }
 
 int *radix_sort_bits(unsigned *keys, int *vals, unsigned *keys2, int *vals2, unsigned *hist, int n, int bits,
                      cudaStream_t st) {
@@ -422,7 +430,7 @@ int *radix_sort_bits(unsigned *keys, int *vals, unsigned *keys2, int *vals2, uns
     const unsigned nblk = (unsigned)((n + kTile - 1) / kTile);
     for (int shift = 0; shift < bits; shift += 4) {
         k_radix_hist<<<nblk, kSortThreads, 0, st>>>(keys, n, shift, hist);
-        k_scan_excl<<<1, kScanThreads, 0, st>>>(hist, kDigits * (int)nblk, nullptr);
+        k_scan_excl<<<kDigits, kScanThreads, 0, st>>>(hist, (int)nblk, hist + (size_t)kDigits * nblk);
         k_radix_scatter<<<nblk, kSortThreads, 0, st>>>(keys, vals, n, shift, hist, keys2, vals2);
         std::swap(keys, keys2);
         std::swap(vals, vals2);

@@ -599,8 +599,11 @@ DT_D int sample_reuse(const double *cdf, int n, double &u, double &pdf) {
 
 // shape.cpp:302-335, in FP64. The side of each face plane is the sign of the dot product
 // with the face's unnormalised normal (normalising by a positive length keeps the sign).
+// Callers test only > 0, which holds for every edge of a mesh without vertex normals (the
+// result is then 2 or 1): such meshes skip the face tests.
 DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) {
     if (e.f0 < 0 || e.f1 < 0) return 2;
+    if (!sc.shapes[e.shape].has_normals) return 1;
     const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
     bool ff[2] = {false, false};
     for (int k = 0; k < 2; ++k) {
@@ -622,29 +625,36 @@ DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) 
 // volpathAD.cpp:231-280 / 540-589 (ALTERNATIVE_EDGE_SAMPLING): the edge point seen from x0
 // at parameter t, by angular interpolation between the edge's endpoints, in FP64 (near-
 // degenerate triangles cancel). w0 : wb = sin(theta (1 - t)) / l0 : sin(theta t) / l1,
-// normalised to a sum of 1; pdf is divided by theta.
+// normalised to a sum of 1; pdf is divided by theta. theta = acos(cos theta) as in the
+// reference; sin(theta t) and cos(theta t) come from one sincos and sin(theta (1 - t)) =
+// sin(theta) cos(theta t) - cos(theta) sin(theta t), with sin(theta) = |e0 x e1| / (l0 l1).
 struct EdgePoint {
     double3_ w1, nrm;   // unit direction to the edge point, unit normal of (x0, v0, v1)
-    double dist, w0, wb;
+    double dist, inv_dist, w0, wb;
 };
 DT_D bool edge_point_solve(const DevScene &sc, const DevEdge &e, const double3_ &x0, double t, double &pdf,
                            EdgePoint &ep) {
     const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
     const double3_ e0 = v0 - x0, e1 = v1 - x0;
-    ep.nrm = normalized(crossd(e0, e1));
-    const double l0 = lengthd(e0), l1 = lengthd(e1);
-    const double c = fmin(1.0, fmax(-1.0, dotd(e0, e1) / (l0 * l1)));
+    const double3_ cr = crossd(e0, e1);
+    const double lc = lengthd(cr);
+    ep.nrm = cr * (1.0 / lc);
+    const double l0 = lengthd(e0), l1 = lengthd(e1), inv_l01 = 1.0 / (l0 * l1);
+    const double c = fmin(1.0, fmax(-1.0, dotd(e0, e1) * inv_l01));
     const double theta = acos(c);
     if (theta < kEpsD || theta > kPiD - kEpsD) return false;
+    double st, ct;
+    sincos(theta * t, &st, &ct);
     // the common factor 1 / sin(theta) of both weights cancels in the normalisation
-    double w0 = sin(theta * (1.0 - t)) * l1, wb = sin(theta * t) * l0;
+    double w0 = (lc * inv_l01 * ct - c * st) * l1, wb = st * l0;
     const double inv = 1.0 / (w0 + wb);
     w0 *= inv;
     wb *= inv;
     if (w0 < -kEpsD || wb < -kEpsD || fabs(w0 + wb - 1.0) > kEpsD) return false;
     const double3_ w = e0 * w0 + e1 * wb;
     ep.dist = lengthd(w);
-    ep.w1 = w * (1.0 / ep.dist);
+    ep.inv_dist = 1.0 / ep.dist;
+    ep.w1 = w * ep.inv_dist;
     ep.w0 = w0;
     ep.wb = wb;
     pdf /= theta;
@@ -660,7 +670,7 @@ template <int N>
 DT_D bool edge_point_slots(const DevScene &sc, const DevEdge &e, const EdgePoint &ep, const float (*x0d)[3], double k2,
                            float *s) {
     const float3 w1 = tof(ep.w1), nrm = tof(ep.nrm);
-    const float w0 = (float)ep.w0, wb = (float)ep.wb, inv_d = (float)(1.0 / ep.dist), k2f = (float)k2;
+    const float w0 = (float)ep.w0, wb = (float)ep.wb, inv_d = (float)ep.inv_dist, k2f = (float)k2;
     const float off_plane = (float)fabs(1.0 - dotd(ep.w1, ep.w1)) * inv_d;
     float mx = 0.f;
     bool moves = false;
@@ -707,8 +717,9 @@ DT_D float3 edge_subpath_dir(const EdgePoint &ep, int sgn) {
     return normalize(tof(ep.w1) + tof(ep.nrm) * a);
 }
 
+// eight resident blocks per SM: the kernel waits on the FP64 pipe and on traversal latency
 template <int N>
-__global__ void __launch_bounds__(kBlock) k_edge(DevScene sc, RenderParams rp, Queue qe, long long rec_begin,
+__global__ void __launch_bounds__(kBlock, 8) k_edge(DevScene sc, RenderParams rp, Queue qe, long long rec_begin,
                                                  long long rec_count, Queue qli, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;

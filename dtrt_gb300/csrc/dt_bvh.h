@@ -46,7 +46,7 @@ struct DeviceBvh {
 // build on the host instead).
 int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBvh &out, std::string &err);
 
-// Stable sort of n (key, value) pairs by the low `bits` bits of the key on stream st (4-bit
+// Stable sort of n (key, value) pairs by the low `bits` bits of the key on stream st (8-bit
 // LSD passes of the BVH build's radix sort). keys2 / vals2 hold n entries, hist
 // radix_hist_entries(n). Returns the values in key order: vals after an even number of
 // passes, vals2 after an odd one.

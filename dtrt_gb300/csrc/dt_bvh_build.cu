@@ -5,9 +5,10 @@
 //   1. per triangle: bounds, centroid; the centroid bounds of the scene (block reduction,
 //      one atomic per block on order-preserving integer images of the floats)
 //   2. 30-bit Morton code of each centroid in those bounds
-//   3. stable LSD radix sort of (code, triangle) pairs, 4 bits per pass: block digit
-//      histograms, one exclusive scan, a scatter whose in-block ranks come from
-//      __match_any_sync (so equal digits keep their order)
+//   3. stable LSD radix sort of (code, triangle) pairs, 8 bits per pass: block digit
+//      histograms, an exclusive scan of each digit's row (one block per digit) and of the
+//      row totals, a scatter whose in-block ranks come from __match_any_sync (so equal
+//      digits keep their order)
 //   4. the binary radix tree of the sorted codes (one thread per inner node; equal codes
 //      are told apart by their sorted position), each node covering a contiguous range
 //   5. node boxes bottom-up: one thread per leaf climbs while it is the second child to
@@ -35,7 +36,8 @@ constexpr int kLeafMax = 4;         // triangles per leaf (3-bit count field all
 constexpr int kSortThreads = 256;   // radix sort block
 constexpr int kSortRounds = 8;      // elements per thread per block tile
 constexpr int kTile = kSortThreads * kSortRounds;
-constexpr int kDigits = 16;         // 4-bit digits
+constexpr int kDigitBits = 8;       // 8-bit digits: 3 passes for the Li and primary-edge sort keys, 4 for Morton codes
+constexpr int kDigits = 1 << kDigitBits;
 constexpr int kScanThreads = 1024;
 
 // order-preserving unsigned image of a float (for atomicMin / atomicMax)
@@ -120,7 +122,7 @@ __global__ void k_morton(const float *tv, int n, const unsigned *bounds, unsigne
 // 3a. digit histogram of each block tile: hist[digit * nblocks + block]
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned *keys, int n, int shift, unsigned *hist) {
     __shared__ unsigned s_cnt[kDigits];
-    if (threadIdx.x < kDigits) s_cnt[threadIdx.x] = 0;
+    for (int q = threadIdx.x; q < kDigits; q += kSortThreads) s_cnt[q] = 0;
     __syncthreads();
     const long long base = (long long)blockIdx.x * kTile;
     for (int r = 0; r < kSortRounds; ++r) {
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const unsigned *key
         if (i < n) atomicAdd(&s_cnt[(keys[i] >> shift) & (kDigits - 1)], 1u);
     }
     __syncthreads();
-    if (threadIdx.x < kDigits) hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = s_cnt[threadIdx.x];
+    for (int q = threadIdx.x; q < kDigits; q += kSortThreads) hist[(size_t)q * gridDim.x + blockIdx.x] = s_cnt[q];
 }
 
 // exclusive scan of m entries per block (m is at most a few hundred thousand): block b scans
@@ -159,7 +161,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_excl(unsigned *a, int m, 
 
 // 3b. stable scatter of each tile by digit, rounds in element order, ranks within a warp
 // from __match_any_sync and across warps from per-warp digit counts. hist holds each
-// digit's row of block counts scanned within the row, then the kDigits row totals.
+// digit's row of block counts scanned within the row, then the digits' exclusive offsets
+// (the row totals scanned).
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned *keys, const int *vals, int n, int shift,
                                                                 const unsigned *hist, unsigned *keys_out,
                                                                 int *vals_out) {
@@ -167,12 +170,8 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned *
     __shared__ unsigned s_base[kDigits];
     __shared__ unsigned s_wcnt[kWarps][kDigits];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (threadIdx.x < kDigits) {
-        const unsigned *totals = hist + (size_t)kDigits * gridDim.x;
-        unsigned digit_base = 0;
-        for (int q = 0; q < (int)threadIdx.x; ++q) digit_base += totals[q];
-        s_base[threadIdx.x] = hist[(size_t)threadIdx.x * gridDim.x + blockIdx.x] + digit_base;
-    }
+    for (int q = threadIdx.x; q < kDigits; q += kSortThreads)
+        s_base[q] = hist[(size_t)q * gridDim.x + blockIdx.x] + hist[(size_t)kDigits * gridDim.x + q];
     const long long base = (long long)blockIdx.x * kTile;
     for (int r = 0; r < kSortRounds; ++r) {
         const long long i = base + (long long)r * kSortThreads + threadIdx.x;
@@ -182,7 +181,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned *
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const unsigned rank = __popc(peers & ((1u << lane) - 1u));
         __syncthreads();  // s_base / s_wcnt of the previous round consumed
-        if (lane < kDigits) s_wcnt[w][lane] = 0;
+        for (int q = lane; q < kDigits; q += 32) s_wcnt[w][q] = 0;
         __syncwarp();
         if (live && rank == 0) s_wcnt[w][d] = __popc(peers);
         __syncthreads();
@@ -192,10 +191,10 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const unsigned *
             for (int ww = 0; ww < w; ++ww) off += s_wcnt[ww][d];
         }
         __syncthreads();
-        if (threadIdx.x < kDigits) {
+        for (int q = threadIdx.x; q < kDigits; q += kSortThreads) {
             unsigned tot = 0;
-            for (int ww = 0; ww < kWarps; ++ww) tot += s_wcnt[ww][threadIdx.x];
-            s_base[threadIdx.x] += tot;
+            for (int ww = 0; ww < kWarps; ++ww) tot += s_wcnt[ww][q];
+            s_base[q] += tot;
         }
         if (live) {
             keys_out[off + rank] = k;
@@ -375,10 +374,10 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
     if (e == cudaSuccess) {
         k_centroid_bounds<<<g, T, 0, st>>>(tv, n, bounds);
         k_morton<<<g, T, 0, st>>>(tv, n, bounds, keys, vals);
-        for (int pass = 0; pass < 8; ++pass) {  // 32 key bits, 4 per pass
-            const int shift = 4 * pass;
+        for (int shift = 0; shift < 32; shift += kDigitBits) {  // 32 key bits
             k_radix_hist<<<nblk, kSortThreads, 0, st>>>(keys, n, shift, hist);
             k_scan_excl<<<kDigits, kScanThreads, 0, st>>>(hist, nblk, hist + (size_t)kDigits * nblk);
+            k_scan_excl<<<1, kScanThreads, 0, st>>>(hist + (size_t)kDigits * nblk, kDigits, nullptr);
             k_radix_scatter<<<nblk, kSortThreads, 0, st>>>(keys, vals, n, shift, hist, keys2, vals2);
             std::swap(keys, keys2);
             std::swap(vals, vals2);
@@ -428,9 +427,10 @@ int *radix_sort_bits(unsigned *keys, int *vals, unsigned *keys2, int *vals2, uns
                      cudaStream_t st) {
     if (n <= 1) return vals;
     const unsigned nblk = (unsigned)((n + kTile - 1) / kTile);
-    for (int shift = 0; shift < bits; shift += 4) {
+    for (int shift = 0; shift < bits; shift += kDigitBits) {
         k_radix_hist<<<nblk, kSortThreads, 0, st>>>(keys, n, shift, hist);
         k_scan_excl<<<kDigits, kScanThreads, 0, st>>>(hist, (int)nblk, hist + (size_t)kDigits * nblk);
+        k_scan_excl<<<1, kScanThreads, 0, st>>>(hist + (size_t)kDigits * nblk, kDigits, nullptr);
         k_radix_scatter<<<nblk, kSortThreads, 0, st>>>(keys, vals, n, shift, hist, keys2, vals2);
         std::swap(keys, keys2);
         std::swap(vals, vals2);

@@ -43,6 +43,15 @@ WORKLOADS = {
 }
 
 
+def workload_config(name, world, spec=None):
+    """The `config` of both arms' lines: the workload, its sizes and the run's layout."""
+    wl = WORKLOADS[name]
+    return {"workload": wl["desc"], "width": spec.width if spec else wl["w"],
+            "height": spec.height if spec else wl["h"], "spp": wl["spp"], "max_bounces": wl["depth"],
+            "nder": wl["nder"], "sppse": wl["sppse"], "sppe": wl["sppe"], "parallelism": f"replicas x{world}",
+            "l2": "flushed between timed steps (256 MiB write)", "accumulation": "f64"}
+
+
 def build_spec(name, size=None):
     """The workload scene; `size` overrides the image side (small ncu captures only)."""
     from dtrt_gb300 import scenes
@@ -170,8 +179,7 @@ def run_reference(args, wl_name, rank):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "paths/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene generator)",
-            "config": {"workload": wl["desc"], "width": wl["w"], "height": wl["h"], "spp": wl["spp"],
-                       "max_bounces": wl["depth"], "nder": wl["nder"], "sppse": wl["sppse"], "sppe": wl["sppe"]},
+            "config": workload_config(wl_name, args.gpus),
             "cpu_baseline": {"value": v, "unit": "paths/s", "cores": cores, "kind": "port",
                              "sample": sample, "cpu": cpu_model()},
             "e2e": {"value": v, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -295,10 +303,7 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     line = {"metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-            "config": {"workload": wl["desc"], "width": spec.width, "height": spec.height, "spp": wl["spp"],
-                       "max_bounces": wl["depth"], "nder": wl["nder"], "sppse": wl["sppse"], "sppe": wl["sppe"],
-                       "parallelism": f"replicas x{world}", "l2": "flushed between timed steps (256 MiB write)",
-                       "accumulation": "f64"},
+            "config": workload_config(wl_name, world, spec),
             "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "derivative_samples_per_s": value * wl["nder"],
             "stages_ms_per_step": {k: v / args.steps for k, v in stage.items()},

@@ -489,8 +489,8 @@ DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
 // After a vertex of level L: a continuing path draws the random numbers and samples the
 // distance of level L+1 right away and is queued as a volume or interface vertex of L+1.
 template <int N>
-DT_D void camera_next(const DevScene &sc, CamState<N> &st, bool alive, VertexIn<N> *vins, int id, int *qv,
-                      unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, Ctr &c) {
+DT_D int camera_next(const DevScene &sc, CamState<N> &st, bool alive, VertexIn<N> *vins, int id, int *qv,
+                     unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, Ctr &c) {
     int kind = 0;
     if (alive && st.mode != 0) {
         VertexIn<N> vin;
@@ -499,6 +499,28 @@ DT_D void camera_next(const DevScene &sc, CamState<N> &st, bool alive, VertexIn<
     }
     push_path(qv, cnt_v, id, kind == 1);
     push_path(qs, cnt_s, id, kind == 2);
+    return kind;
+}
+
+// The path state its next launch reads: all of it before an interface vertex; all but the
+// hit record before a volume vertex (which writes the record without reading it); the sums
+// alone when the path has ended (k_cam_accum reads nothing else).
+template <int N>
+DT_D void store_state(CamState<N> *states, int id, const CamState<N> &st, int next_kind) {
+    CamState<N> &d = states[id];
+    if (next_kind == 2) {
+        d = st;
+        return;
+    }
+    d.acc = st.acc;
+    if (next_kind == 0) return;
+    d.rng = st.rng;
+    d.ray = st.ray;
+    d.P = st.P;
+    d.med = st.med;
+    d.depth = st.depth;
+    d.mode = st.mode;
+    d.level = st.level;
 }
 
 // Path start and level 0: primary ray, first hit, the level's random numbers and distance
@@ -530,8 +552,8 @@ __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams 
         }
     }
     push_path(qv0, cnt_v0, (int)gi, kind == 1);
-    camera_next<N>(sc, st, next, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
-    if (gi < rp.path_count) states[gi] = st;
+    const int nk = camera_next<N>(sc, st, next, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    if (gi < rp.path_count) store_state<N>(states, (int)gi, st, kind == 1 ? 1 : nk);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
 
@@ -550,14 +572,29 @@ __global__ void __launch_bounds__(kBlock) k_cam_vertex(DevScene sc, RenderParams
     Ctr c;
     for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
         const int id = q_in[i];
-        CamState<N> st = states[id];
+        CamState<N> st;
+        if (kVolume) {
+            // a volume vertex writes the hit record (of its continuation) without reading it:
+            // the record stays in HBM (380 B of 848 at nder 8)
+            const CamState<N> &s0 = states[id];
+            st.rng = s0.rng;
+            st.ray = s0.ray;
+            st.P = s0.P;
+            st.acc = s0.acc;
+            st.med = s0.med;
+            st.depth = s0.depth;
+            st.mode = s0.mode;
+            st.level = s0.level;
+        } else {
+            st = states[id];
+        }
         const VertexIn<N> vin = vins[id];
         const long long g = rp.path_begin + id;
         const bool alive = kVolume ? camera_volume<N>(sc, rp, stack, g, st, vin, qe, c)
                                    : camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c);
         ++st.level;
-        camera_next<N>(sc, st, alive, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next, c);
-        states[id] = st;
+        const int nk = camera_next<N>(sc, st, alive, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next, c);
+        store_state<N>(states, id, st, nk);
     }
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
@@ -572,11 +609,6 @@ __global__ void __launch_bounds__(kBlock) k_cam_accum(RenderParams rp, const Cam
 }
 
 // ====================================================================== FP64 edge geometry
-struct EdgeGeom {
-    double w1[3], nrm[3];
-    double dist, pdf;
-};
-
 // pmf.h:103-167 sampleReuse on a normalised CDF with a leading 0 (n+1 entries). The CDF
 // entries and u are non-negative doubles, whose IEEE bit patterns order as 64-bit integers:
 // the search compares those on the integer pipe and leaves the FP64 pipe (1/64 of FP32 on

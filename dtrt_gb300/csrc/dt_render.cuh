@@ -190,11 +190,16 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                     DT_CK(cudaMemcpyAsync(lc.data(), vcnt, lc.size() * sizeof(unsigned long long),
                                           cudaMemcpyDeviceToHost, st));
                     DT_CK(cudaStreamSynchronize(st));
-                    const uint64_t sv = sizeof(CamState<N>) + sizeof(VertexIn<N>);
-                    uint64_t launched = 0;
-                    for (int L = 0; L < levels; ++L) launched += lc[L] + (L > 0 ? lc[levels + 1 + L] : 0);
-                    state_traffic += 2 * sv * launched + sv * (uint64_t)rp.path_count +
-                                   sizeof(DV<N>) * (uint64_t)rp.path_count;
+                    // each queued vertex's state and inputs are written once and read once (a
+                    // volume vertex's without the hit record); an ended path writes its sums,
+                    // which k_cam_accum reads
+                    const uint64_t sv = sizeof(CamState<N>) + sizeof(VertexIn<N>), si = sizeof(ItsAD<N>);
+                    uint64_t vol = 0, itf = 0;
+                    for (int L = 0; L < levels; ++L) {
+                        vol += lc[L];
+                        itf += L > 0 ? lc[levels + 1 + L] : 0;
+                    }
+                    state_traffic += 2 * ((sv - si) * vol + sv * itf) + 2 * sizeof(DV<N>) * (uint64_t)rp.path_count;
                 }
             } else if ((rc = timed(ms_camera, [&] {
                             k_camera<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, qe, ql, sb.acc1, ctr);

@@ -448,7 +448,7 @@ def grad_rmse_c3(size=None, runs=16, run_spp=64, ladder_max=64, seed=31, ref_spp
     brng = np.random.default_rng(0)
     boots = sorted(spp_1pct(G[brng.integers(0, runs, runs)]) for _ in range(200))
     t_var = time.perf_counter() - t0
-    # high-spp forward-mode reference (the benchmark spec's oracle for the gradient), bias included
+    # high-spp forward-mode reference for the gradient (the run mean's bias is measured against it)
     g_ref = forward_mode(ref_spp, 777)[0]
     result = {"workload": f"C3 {W}x{H}, {res}^3 grid, depth {depth}, L2 loss vs +-20% amplitude target",
               "against_reference": rmse_summary(G, run_spp, g_ref, ref_spp),

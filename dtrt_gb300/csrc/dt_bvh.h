@@ -51,6 +51,8 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
 // radix_hist_entries(n). Returns the values in key order: vals after an even number of
 // passes, vals2 after an odd one.
 size_t radix_hist_entries(long long n);
+// kernel launches of one radix_sort_bits call (4 per pass)
+int radix_sort_launches(int bits);
 int *radix_sort_bits(unsigned *keys, int *vals, unsigned *keys2, int *vals2, unsigned *hist, int n, int bits,
                      cudaStream_t st);
 

@@ -421,6 +421,8 @@ int build_bvh_device(const std::vector<float> &tri_verts, int num_tris, DeviceBv
     return 0;
 }
 
+int radix_sort_launches(int bits) { return 4 * ((bits + kDigitBits - 1) / kDigitBits); }
+
 size_t radix_hist_entries(long long n) { return (size_t)kDigits * (size_t)((n + kTile - 1) / kTile + 1); }
 
 int *radix_sort_bits(unsigned *keys, int *vals, unsigned *keys2, int *vals2, unsigned *hist, int n, int bits,

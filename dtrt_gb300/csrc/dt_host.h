@@ -47,28 +47,33 @@ inline bool ensure_li_sort(Scratch &sb, uint64_t li_cap) {
 }
 
 // The n queued Li tasks' pairs (slots 2m, 2m + 1) in key order (k_li_keys) on stream st;
-// nullptr when n is odd or holds one pair (the queue is then read in order).
+// nullptr when n is odd or holds one pair (the queue is then read in order). Adds the
+// kernels it launches to `launches`.
 template <class Task>
 const int *sort_li_pairs(const DevScene &sc, const Task *tasks, long long n, Scratch &sb, uint64_t li_cap,
-                         cudaStream_t st) {
+                         cudaStream_t st, uint64_t &launches) {
     const long long np = n / 2, cap = (long long)(li_cap / 2);
     if ((n & 1) || np < 2 || np > cap) return nullptr;
     unsigned *keys = (unsigned *)sb.li_sort, *keys2 = keys + cap;
     int *vals = (int *)(keys2 + cap), *vals2 = vals + cap;
     unsigned *hist = (unsigned *)(vals2 + cap);
     k_li_keys<Task><<<(unsigned)((np + 255) / 256), 256, 0, st>>>(sc, tasks, np, keys, vals);
+    launches += 1 + radix_sort_launches(kLiSortKeyBits);
     return radix_sort_bits(keys, vals, keys2, vals2, hist, (int)np, kLiSortKeyBits, st);
 }
 
 // The primary-edge samples [rp.prim_begin, + rp.prim_count) in key order (k_primary_keys),
 // in the Li sort's buffers (a chunk holds at most li_cap / 2 samples); nullptr for one.
-inline const int *sort_primary_samples(const RenderParams &rp, Scratch &sb, uint64_t li_cap, cudaStream_t st) {
+// Adds the kernels it launches to `launches`.
+inline const int *sort_primary_samples(const RenderParams &rp, Scratch &sb, uint64_t li_cap, cudaStream_t st,
+                                       uint64_t &launches) {
     const long long cap = (long long)(li_cap / 2);
     if (rp.prim_count < 2 || rp.prim_count > cap) return nullptr;
     unsigned *keys = (unsigned *)sb.li_sort, *keys2 = keys + cap;
     int *vals = (int *)(keys2 + cap), *vals2 = vals + cap;
     unsigned *hist = (unsigned *)(vals2 + cap);
     k_primary_keys<<<(unsigned)((rp.prim_count + 255) / 256), 256, 0, st>>>(rp, keys, vals);
+    launches += 1 + radix_sort_launches(20);
     return radix_sort_bits(keys, vals, keys2, vals2, hist, (int)rp.prim_count, 20, st);
 }
 

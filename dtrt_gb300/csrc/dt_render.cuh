@@ -119,7 +119,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         if (n)
             if ((rc = timed(ms_li, [&] {
                      const int *perm = li_sorted ? sort_li_pairs(sc, (const LiTask<N> *)qli.data, (long long)n, sb,
-                                                                 li_cap, st)
+                                                                 li_cap, st, launches)
                                                  : nullptr;
                      k_li<N><<<blocks(n), kBlock, 0, st>>>(sc, rp, qli, 0, n, sb.acc1, sb.acc2, perm, ctr);
                  })))
@@ -236,7 +236,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
             rp.prim_begin = k0;
             rp.prim_count = std::min(chunk, ns - k0);
             if ((rc = timed(ms_primary, [&] {
-                     const int *perm = li_sorted ? sort_primary_samples(rp, sb, li_cap, st) : nullptr;
+                     const int *perm = li_sorted ? sort_primary_samples(rp, sb, li_cap, st, launches) : nullptr;
                      k_primary<N><<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, perm, ctr);
                  })))
                 return rc;

@@ -142,8 +142,9 @@ int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const flo
         const unsigned long long n = std::min<unsigned long long>(hcnt[2], li_cap);
         tot_li += n;
         if (n) {
-            const int *perm = li_sorted ? sort_li_pairs(sc, (const VLiTask *)qli.data, (long long)n, sb, li_cap, st)
-                                        : nullptr;
+            const int *perm =
+                li_sorted ? sort_li_pairs(sc, (const VLiTask *)qli.data, (long long)n, sb, li_cap, st, launches)
+                          : nullptr;
             k_vadj_li<<<blocks((long long)n), kBlock, 0, st>>>(sc, rp, qli, (long long)n, dimg, grad, xadj, perm,
                                                                ctr);
             ++launches;
@@ -189,7 +190,7 @@ int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const flo
         for (long long k0 = 0; k0 < ns; k0 += chunk) {
             rp.prim_begin = k0;
             rp.prim_count = std::min(chunk, ns - k0);
-            const int *perm = li_sorted ? sort_primary_samples(rp, sb, li_cap, st) : nullptr;
+            const int *perm = li_sorted ? sort_primary_samples(rp, sb, li_cap, st, launches) : nullptr;
             k_vadj_primary<<<blocks(rp.prim_count), kBlock, 0, st>>>(sc, rp, qli, perm, ctr);
             ++launches;
             DT_VCK(cudaGetLastError());

@@ -1014,9 +1014,13 @@ DT_HEAVY bool sample_distance_ad(const DevScene &sc, const DevMedium &m, RayAD<N
             set_error(sc, ERR_TRACK_CAP);
             break;
         }
+        // the acceptance test needs the density value only; a null collision discards the
+        // derivative slots, so the dual lookup runs at an accepted collision (same point)
         const DV<N> p = ray.o + ray.d * t;
-        const Df<N> dens = grid_lookup_ad<N>(m.density, p, c);
-        if (rng.next1() * m.density.max_value < dens.v) {
+        const float dv = grid_lookup(m.density, p.val(), c);
+        if (rng.next1() * m.density.max_value < dv) {
+            Ctr again;  // the lookup just counted, repeated with its derivative slots
+            const Df<N> dens = grid_lookup_ad<N>(m.density, p, again);
             // The reference aliases p_scatter with ray.org (volpathAD.cpp:164), so the
             // line integral below runs from the scatter point forward over [0, t].
             // EST_SCATTER_FROM_ORIGIN integrates the segment actually travelled instead.

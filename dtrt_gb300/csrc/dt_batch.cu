@@ -213,8 +213,9 @@ int launch_once(dtrt_batch *b, const std::vector<int> &order, int chunk, long lo
     return rc ? rc : launch_kernel(b, total, chunk, stride, st);
 }
 
-// one k_adjoint launch per item (every stride-th path), items dealt round-robin in `order`
-// to st and S-1 side streams that fork from and join back into st (graph-capturable)
+// one k_adjoint launch per item (every stride-th path), items taken in `order`, each dealt to
+// the least-loaded of st and S-1 side streams that fork from and join back into st (graph-
+// capturable); an item's load is its measured cost estimate, else its path count
 int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long stride, cudaStream_t st,
                  bool zero = false) {
     S = std::max(1, std::min(S, 1 + (int)b->side.size()));
@@ -222,10 +223,14 @@ int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long 
         DT_BCK(cudaEventRecord(b->fork_ev, st));
         for (int k = 1; k < S; ++k) DT_BCK(cudaStreamWaitEvent(b->side[k - 1], b->fork_ev, 0));
     }
+    std::vector<double> load(S, 0.0);
     for (size_t i = 0; i < order.size(); ++i) {
         const int item = order[i];
         const BatchItemDev &it = b->host_items[item];
-        cudaStream_t q = (i % S == 0) ? st : b->side[i % S - 1];
+        const int s = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        const double est = b->stats.item_ms_estimate[std::min(item, DTRT_BATCH_MAX_ITEMS - 1)];
+        load[s] += est > 0.0 ? est : (double)b->paths[item];
+        cudaStream_t q = s == 0 ? st : b->side[s - 1];
         if (zero) {  // each item's outputs are cleared just before its own launches, on its stream
             if (it.img_acc) DT_BCK(cudaMemsetAsync(it.img_acc, 0, b->npix[item] * 3 * 8, q));
             if (it.grad) DT_BCK(cudaMemsetAsync(it.grad, 0, b->nvox[item] * 4, q));
@@ -235,7 +240,7 @@ int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long 
             continue;
         }
         if (!b->wave.empty()) {  // the wavefront replay of dtrt_render_adjoint, on this stream's workspace
-            DT_BCK(launch_adjoint_wave(it.sc, it.rp, it.dimg, it.grad, it.img_acc, nullptr, b->wave[i % S], b->sms, q,
+            DT_BCK(launch_adjoint_wave(it.sc, it.rp, it.dimg, it.grad, it.img_acc, nullptr, b->wave[s], b->sms, q,
                                        nullptr));
             continue;
         }

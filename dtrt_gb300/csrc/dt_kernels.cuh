@@ -33,6 +33,7 @@ struct RenderParams {
     int npix, out_w, out_h, crop_x, crop_y;
     long long path_begin, path_count;
     double prim_weight;  // primary-edge PDF sum / sample count
+    double inv_sppse;    // 1 / sppse (0 when sppse is 0)
     long long prim_begin, prim_count;
 };
 
@@ -657,15 +658,14 @@ DT_D int is_silhouette(const DevScene &sc, const DevEdge &e, const double3_ &p) 
 // volpathAD.cpp:231-280 / 540-589 (ALTERNATIVE_EDGE_SAMPLING): the edge point seen from x0
 // at parameter t, by angular interpolation between the edge's endpoints, in FP64 (near-
 // degenerate triangles cancel). w0 : wb = sin(theta (1 - t)) / l0 : sin(theta t) / l1,
-// normalised to a sum of 1; pdf is divided by theta. theta = acos(cos theta) as in the
+// normalised to a sum of 1; the angular pdf is the edge pdf / theta (theta returned). theta = acos(cos theta) as in the
 // reference; sin(theta t) and cos(theta t) come from one sincos and sin(theta (1 - t)) =
 // sin(theta) cos(theta t) - cos(theta) sin(theta t), with sin(theta) = |e0 x e1| / (l0 l1).
 struct EdgePoint {
     double3_ w1, nrm;   // unit direction to the edge point, unit normal of (x0, v0, v1)
-    double dist, inv_dist, w0, wb;
+    double dist, inv_dist, w0, wb, theta;
 };
-DT_D bool edge_point_solve(const DevScene &sc, const DevEdge &e, const double3_ &x0, double t, double &pdf,
-                           EdgePoint &ep) {
+DT_D bool edge_point_solve(const DevScene &sc, const DevEdge &e, const double3_ &x0, double t, EdgePoint &ep) {
     const double3_ v0 = tod(f3(__ldg(sc.verts + e.v0))), v1 = tod(f3(__ldg(sc.verts + e.v1)));
     const double3_ e0 = v0 - x0, e1 = v1 - x0;
     const double3_ cr = crossd(e0, e1);
@@ -689,7 +689,7 @@ DT_D bool edge_point_solve(const DevScene &sc, const DevEdge &e, const double3_ 
     ep.w1 = w * ep.inv_dist;
     ep.w0 = w0;
     ep.wb = wb;
-    pdf /= theta;
+    ep.theta = theta;
     return true;
 }
 
@@ -765,7 +765,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_edge(DevScene sc, RenderParams rp
         Rng rng;
         rng.init(rp.seed, child_key(r.key, 7u, (uint32_t)i));
         nsamples = 1;
-        double u = ((double)i + rng.next1d()) / rp.sppse;
+        double u = ((double)i + rng.next1d()) * rp.inv_sppse;
         double pdf_shape, pdf_edge;
         const int sid = sample_reuse(sc.shape_edge_cdf, sc.num_shapes, u, pdf_shape);
         const DevShape &shp = sc.shapes[sid];
@@ -779,8 +779,9 @@ __global__ void __launch_bounds__(kBlock, 8) k_edge(DevScene sc, RenderParams rp
                   is_silhouette(sc, e, x0) > 0;
         EdgePoint ep;
         float s[N];
-        if (ok) ok = edge_point_solve(sc, e, x0, u, pdf, ep);
-        if (ok) ok = edge_point_slots<N>(sc, e, ep, r.x0d, 1.0 / (pdf * rp.sppse), s);
+        if (ok) ok = edge_point_solve(sc, e, x0, u, ep);
+        // slot weight factor 1 / (angular pdf * sppse), angular pdf = pdf / theta
+        if (ok) ok = edge_point_slots<N>(sc, e, ep, r.x0d, ep.theta * rp.inv_sppse / pdf, s);
         float3 val = mk(0.f, 0.f, 0.f);
         int med1 = r.med;
         const float3 w1f = ok ? tof(ep.w1) : mk(0.f, 0.f, 1.f);

@@ -40,6 +40,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
     rp.spp = o->spp;
     rp.max_bounces = o->max_bounces;
     rp.sppse = std::max(0, o->sppse);
+    rp.inv_sppse = rp.sppse > 0 ? 1.0 / rp.sppse : 0.0;
     rp.mode = o->mode >= 0 ? o->mode : MODE_ALL;
     rp.jitter = o->sppe >= 0 ? 1 : 0;
     rp.ddist = o->ddist_coeff;
@@ -338,6 +339,7 @@ int render_n_noalloc(dtrt_scene *s, const dtrt_render_options *o, float *out, in
     rp.spp = o->spp;
     rp.max_bounces = o->max_bounces;
     rp.sppse = std::max(0, o->sppse);
+    rp.inv_sppse = rp.sppse > 0 ? 1.0 / rp.sppse : 0.0;
     rp.mode = o->mode >= 0 ? o->mode : MODE_ALL;
     rp.jitter = o->sppe >= 0 ? 1 : 0;
     rp.ddist = o->ddist_coeff;

@@ -69,6 +69,7 @@ int render_vertex_adjoint(dtrt_scene *s, const dtrt_render_options *o, const flo
     rp.spp = o->spp;
     rp.max_bounces = o->max_bounces;
     rp.sppse = std::max(0, o->sppse);
+    rp.inv_sppse = rp.sppse > 0 ? 1.0 / rp.sppse : 0.0;
     rp.mode = o->mode >= 0 ? o->mode : MODE_ALL;
     rp.jitter = o->sppe >= 0 ? 1 : 0;
     rp.ddist = o->ddist_coeff;

@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
         Rng rng;
         rng.init(rp.seed, child_key(r.key, 7u, (uint32_t)i));
         nsamples = 1;
-        double u = ((double)i + rng.next1d()) / rp.sppse;
+        double u = ((double)i + rng.next1d()) * rp.inv_sppse;
         double pdf_shape, pdf_edge;
         const int sid = sample_reuse(sc.shape_edge_cdf, sc.num_shapes, u, pdf_shape);
         const DevShape &shp = sc.shapes[sid];
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
                   !edge_sample_is_zero(sc, r.shape, r.wi, r.fn, r.x0, e) && is_silhouette(sc, e, x0) > 0;
         // the edge-point solve of k_edge: direction, pdf and interpolation weights
         EdgePoint ep;
-        if (ok) ok = edge_point_solve(sc, e, x0, u, pdf, ep);
+        if (ok) ok = edge_point_solve(sc, e, x0, u, ep);
         const double3_ w1 = ok ? ep.w1 : mkd(0.0, 0.0, 1.0), nrm = ok ? ep.nrm : mkd(0.0, 0.0, 1.0);
         const double dist = ok ? ep.dist : 0.0, w0 = ok ? ep.w0 : 0.0, wb = ok ? ep.wb : 0.0;
         float3 val = mk(0.f, 0.f, 0.f);
@@ -354,7 +354,8 @@ __global__ void __launch_bounds__(kBlock) k_vadj_edge(DevScene sc, RenderParams 
         }
         if (ok) {
             // s(V) = m . (w0 dv0 + wb dv1 - dx0), m = (n_e - (n_e.w1) w1) / (dist pdf sppse)
-            const double nw = dotd(nrm, w1), k2 = 1.0 / (dist * pdf * rp.sppse);
+            // 1 / (dist * angular pdf * sppse), angular pdf = pdf / theta
+            const double nw = dotd(nrm, w1), k2 = ep.theta * rp.inv_sppse / (dist * pdf);
             const double3_ m = (nrm - w1 * nw) * k2;
             const float3 c0 = tof(m * w0), c1 = tof(m * wb), cx = tof(m * (-(w0 + wb)));
             const long long slot = queue_reserve_n(sc, qli, 2);  // the pair in adjacent slots

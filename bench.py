@@ -288,7 +288,8 @@ def run_gpu(args, wl_name, rank, world, local_rank):
     value, t_max = job_throughput(paths_per_step, args.steps, world, ms, "cuda")
     # end to end through the public API with host buffers: scene upload + BVH build + render + D2H
     e2e_steps = max(1, min(args.steps, 3))
-    host_out = np.zeros(spec.out_shape(), np.float32)
+    host_t = torch.zeros(spec.out_shape(), dtype=torch.float32).pin_memory()  # pinned result buffer
+    host_out = host_t.numpy()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_steps):

@@ -687,7 +687,7 @@ def batch_c4(n=64, side_scale=1.0, spp_scale=1.0, reps=2, tune_full=True):
             "tune_and_capture_s": tune_s, "schedule": st["schedule"], "streams": st["streams"],
             "chunk_paths": st["chunk_paths"],
             "order_longest_first": st["order_longest_first"], "grid_blocks": st["grid_blocks"],
-            "full_size_trials_ms": st["full_size_ms"], "reps_ms": {"one_at_a_time": t_seq, "batch": t_batch},
+            "confirm_trials_ms_quarter_of_items": st["full_size_ms"], "reps_ms": {"one_at_a_time": t_seq, "batch": t_batch},
             "clocks": clk, "trials": st["trials"]}
 
 

@@ -134,6 +134,7 @@ struct dtrt_batch {
     // the batch wavefront (schedule 2): one replay wavefront over the paths of all items
     void *bw_mem = nullptr;
     dt::AdjWave bw;
+    int wave_items = 0;  // items in the uploaded wavefront numbering
     int max_levels = 1;
     bool any_grad = false;
     // tuning: best strided-sample time of the persistent launch, the per-item schedule on
@@ -258,12 +259,15 @@ int launch_items(dtrt_batch *b, const std::vector<int> &order, int S, long long 
     return DTRT_OK;
 }
 
-// the batch wavefront's path numbering: items in `order`, every stride-th path (blocking
-// copies: never inside a stream capture). Returns the number of global paths.
+// the batch wavefront's path numbering: the items in `order` (all of them, or a subset),
+// every stride-th path (blocking copies: never inside a stream capture). Returns the number
+// of global paths.
 int upload_wave_layout(dtrt_batch *b, const std::vector<int> &order, long long stride, long long &total) {
-    std::vector<long long> gbeg(b->n + 1, 0);
-    for (int i = 0; i < b->n; ++i) gbeg[i + 1] = gbeg[i] + (b->paths[order[i]] + stride - 1) / stride;
-    total = gbeg[b->n];
+    const int m = (int)order.size();
+    std::vector<long long> gbeg(m + 1, 0);
+    for (int i = 0; i < m; ++i) gbeg[i + 1] = gbeg[i] + (b->paths[order[i]] + stride - 1) / stride;
+    total = gbeg[m];
+    b->wave_items = m;
     DT_BCK(cudaMemcpy(b->d_cbeg, gbeg.data(), gbeg.size() * 8, cudaMemcpyHostToDevice));
     DT_BCK(cudaMemcpy(b->d_order, order.data(), order.size() * 4, cudaMemcpyHostToDevice));
     return DTRT_OK;
@@ -315,7 +319,7 @@ int enqueue_wave(dtrt_batch *b, long long total, long long stride, cudaStream_t 
         DT_BCK(cudaEventRecord(b->fork_ev, st));
         for (int k = 1; k < S; ++k) DT_BCK(cudaStreamWaitEvent(b->side[k - 1], b->fork_ev, 0));
     }
-    BatchWave bw{b->d_items, b->d_cbeg, b->d_order, b->n, 0, 0, stride};
+    BatchWave bw{b->d_items, b->d_cbeg, b->d_order, b->wave_items, 0, 0, stride};
     int k = 0;
     for (long long b0 = 0; b0 < total; b0 += cap, k = (k + 1) % S) {
         bw.begin = b0;
@@ -484,7 +488,8 @@ int autotune(dtrt_batch *b, cudaStream_t st) {
 // Full-size confirmation (DTRT_BATCH_TUNE_FULL): a strided sample shrinks every per-item
 // launch to a few waves, which understates that schedule on large items. The two
 // candidates (persistent, per-item on 1, 2 or 4 streams, batch wavefront) that were
-// fastest on the sample run once each on the whole batch; the faster one is kept.
+// fastest on the sample run once each on whole items, every fourth in cost order; the
+// faster one is kept.
 int autotune_full(dtrt_batch *b, cudaStream_t st) {
     const int saved_chunk = b->chunk;
     const std::vector<int> saved_order = b->order;
@@ -498,7 +503,13 @@ int autotune_full(dtrt_batch *b, cudaStream_t st) {
     int best_sched = 0, best_streams = 1;
     std::vector<int> natural(b->n);
     std::iota(natural.begin(), natural.end(), 0);
-    // the two best candidates on the strided sample are confirmed at full size. With items
+    // whole items (not a strided sample of paths), every fourth in cost order from 8 items
+    // on: the wavefront schedules see full-size launches at a quarter of the batch's work
+    std::vector<int> sub_longest, sub_natural;
+    for (int i = 0; i < b->n; i += b->n >= 8 ? 4 : 1) sub_longest.push_back(longest[i]);
+    sub_natural = sub_longest;
+    std::sort(sub_natural.begin(), sub_natural.end());
+    // the two best candidates on the strided sample are confirmed on those items. With items
     // large enough for the wavefront replay the persistent megakernel is left out: the
     // strided sample understates the wavefront schedules (a sample of a large item is a few
     // short launches) and overstates the megakernel, which the replay wavefront outpaces
@@ -519,14 +530,18 @@ int autotune_full(dtrt_batch *b, cudaStream_t st) {
         DT_BCK(cudaStreamSynchronize(st));
         int rc;
         if (cand == 4) {
-            rc = timed(st, [&]() { return launch_wave(b, natural, 1, st); }, ms);
-        } else if (cand == 0) {
+            rc = timed(st, [&]() { return launch_wave(b, sub_natural, 1, st); }, ms);
+        } else if (cand == 0) {  // the persistent layout covers every item
             long long total = 0;
             rc = upload_layout(b, saved_order, saved_chunk, 1, total);
             if (rc) return rc;
             rc = timed(st, [&]() { return launch_kernel(b, total, saved_chunk, 1, st); }, ms);
+            double all = 0.0, part = 0.0;  // scaled to the subset's share of the estimated cost
+            for (int i = 0; i < b->n; ++i) all += b->stats.item_ms_estimate[std::min(i, DTRT_BATCH_MAX_ITEMS - 1)];
+            for (int i : sub_longest) part += b->stats.item_ms_estimate[std::min(i, DTRT_BATCH_MAX_ITEMS - 1)];
+            if (all > 0.0) ms = (float)(ms * part / all);
         } else {
-            rc = timed(st, [&]() { return launch_items(b, longest, 1 << (cand - 1), 1, st); }, ms);
+            rc = timed(st, [&]() { return launch_items(b, sub_longest, 1 << (cand - 1), 1, st); }, ms);
         }
         if (rc) return rc;
         if (cand < 4) b->stats.full_ms[cand] = ms;

@@ -396,7 +396,7 @@ typedef struct {
 
 #define DTRT_BATCH_AUTOTUNE 1u /* measure item costs and pick item order and chunk size */
 #define DTRT_BATCH_GRAPH 2u    /* capture the launch in a CUDA graph */
-#define DTRT_BATCH_TUNE_FULL 4u /* also time the candidate schedules once each on the whole batch */
+#define DTRT_BATCH_TUNE_FULL 4u /* also time the two best sampled schedules on whole items (every fourth by cost) */
 #define DTRT_BATCH_WAVEFRONT 8u /* one replay wavefront over the paths of all items, without tuning */
 #define DTRT_BATCH_MAX_ITEMS 256
 #define DTRT_BATCH_MAX_TRIALS 16
@@ -416,8 +416,9 @@ typedef struct {
                                               trial_chunk < 0: per-item schedule on -chunk streams,
                                               trial_chunk == 0: the batch wavefront */
     int64_t tune_sample_stride;
-    float full_ms[4];               /* DTRT_BATCH_TUNE_FULL: persistent, per-item on 1, 2, 4 streams
-                                       (-1: not confirmed; the two best on the strided sample are) */
+    float full_ms[4];               /* DTRT_BATCH_TUNE_FULL: persistent, per-item on 1, 2, 4 streams, on
+                                       every fourth item by cost (-1: not confirmed; the two best on
+                                       the strided sample are) */
     double item_ms_estimate[DTRT_BATCH_MAX_ITEMS]; /* measured cost of each item (probe) */
     int order[DTRT_BATCH_MAX_ITEMS];
     float full_ms_wavefront;        /* DTRT_BATCH_TUNE_FULL: the batch wavefront (-1: not confirmed) */

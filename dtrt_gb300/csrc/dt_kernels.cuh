@@ -14,9 +14,12 @@
 //   k_edge     one thread per (edge record, edge sample): FP64 silhouette test and
 //              edge-point solve, the visibility gate, then two LiTask sub-paths
 //   k_lins     one thread per Lins record: the Lins estimate with its Li sub-paths
-//   k_primary  one thread per primary-edge sample (integratorAD.cpp:100-165)
+//   k_primary  one thread per primary-edge sample (integratorAD.cpp:100-165), samples
+//              taken in the order of their edge-selecting random number (k_primary_keys)
 //   k_li       one thread per LiTask: the non-AD path Li (volpathAD.cpp:50-142), whose
-//              result L adds s_j * w_c * L_c to derivative slot j of its pixel
+//              result L adds s_j * w_c * L_c to derivative slot j of its pixel; the two
+//              sub-paths of a sample sit in adjacent slots and the pairs are read in the
+//              order of their origin / direction cell (k_li_keys + radix sort)
 //   k_finalize FP64 accumulators -> float image with the reference's write rules
 //
 // All pushes are warp-aggregated (ballot + popc, one atomic per warp); a push past a

@@ -490,19 +490,43 @@ DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = id;  // at most one push per path and level
 }
 
+// push from the back of a queue of `cap` slots: entry k at q[cap - 1 - k]
+DT_D void push_path_back(int *q, long long cap, unsigned long long *count, int id, bool pred) {
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (pred) q[cap - 1 - (long long)(base + __popc(m & ((1u << lane) - 1u)))] = id;
+}
+
+// Interface vertices of a level share one queue of `cap` slots: a hit on a diffuse or Phong
+// surface is pushed from the front, a hit on a null or rough-dielectric surface from the
+// back, so that the warps of the level's launch run one BSDF's branches (at most one warp
+// mixes them). Each path is pushed at most once per level: the two ends never meet.
+DT_D bool interface_back(const DevScene &sc, int shape) {
+    const int t = sc.bsdfs[sc.shapes[shape].bsdf_id].type;
+    return t == BSDF_NULL || t == BSDF_ROUGHDIELECTRIC;
+}
+
 // After a vertex of level L: a continuing path draws the random numbers and samples the
 // distance of level L+1 right away and is queued as a volume or interface vertex of L+1.
 template <int N>
 DT_D int camera_next(const DevScene &sc, CamState<N> &st, bool alive, VertexIn<N> *vins, int id, int *qv,
-                     unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, Ctr &c) {
+                     unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, unsigned long long *cnt_s_back,
+                     long long cap, Ctr &c) {
     int kind = 0;
     if (alive && st.mode != 0) {
         VertexIn<N> vin;
         kind = camera_decide<N>(sc, st, vin, c);
         if (kind) vins[id] = vin;
     }
+    const bool back = kind == 2 && interface_back(sc, st.its.shape);
     push_path(qv, cnt_v, id, kind == 1);
-    push_path(qs, cnt_s, id, kind == 2);
+    push_path(qs, cnt_s, id, kind == 2 && !back);
+    push_path_back(qs, cap, cnt_s_back, id, back);
     return kind;
 }
 
@@ -534,8 +558,8 @@ template <int N>
 __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams rp, CamState<N> *states,
                                                       VertexIn<N> *vins, int *qv0, unsigned long long *cnt_v0,
                                                       int *qv1, unsigned long long *cnt_v1, int *qs1,
-                                                      unsigned long long *cnt_s1, Queue qe, Queue ql,
-                                                      unsigned long long *ctr) {
+                                                      unsigned long long *cnt_s1, unsigned long long *cnt_s1_back,
+                                                      long long cap, Queue qe, Queue ql, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
@@ -556,7 +580,7 @@ __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams 
         }
     }
     push_path(qv0, cnt_v0, (int)gi, kind == 1);
-    const int nk = camera_next<N>(sc, st, next, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    const int nk = camera_next<N>(sc, st, next, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, cnt_s1_back, cap, c);
     if (gi < rp.path_count) store_state<N>(states, (int)gi, st, kind == 1 ? 1 : nk);
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
@@ -566,16 +590,18 @@ __global__ void __launch_bounds__(kBlock) k_cam_start(DevScene sc, RenderParams 
 template <int N, bool kVolume>
 __global__ void __launch_bounds__(kBlock) k_cam_vertex(DevScene sc, RenderParams rp, CamState<N> *states,
                                                        VertexIn<N> *vins, const int *q_in,
-                                                       const unsigned long long *cnt_in, int *qv_next,
+                                                       const unsigned long long *cnt_in,
+                                                       const unsigned long long *cnt_in_back, int *qv_next,
                                                        unsigned long long *cnt_v_next, int *qs_next,
-                                                       unsigned long long *cnt_s_next, Queue qe, Queue ql,
-                                                       unsigned long long *ctr) {
+                                                       unsigned long long *cnt_s_next,
+                                                       unsigned long long *cnt_s_next_back, long long cap, Queue qe,
+                                                       Queue ql, unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
-    const long long n = (long long)*cnt_in;
+    const long long nf = (long long)*cnt_in, n = nf + (cnt_in_back ? (long long)*cnt_in_back : 0);
     Ctr c;
     for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
-        const int id = q_in[i];
+        const int id = i < nf ? q_in[i] : q_in[cap - 1 - (i - nf)];
         CamState<N> st;
         if (kVolume) {
             // a volume vertex writes the hit record (of its continuation) without reading it:
@@ -597,7 +623,8 @@ __global__ void __launch_bounds__(kBlock) k_cam_vertex(DevScene sc, RenderParams
         const bool alive = kVolume ? camera_volume<N>(sc, rp, stack, g, st, vin, qe, c)
                                    : camera_surface<N>(sc, rp, stack, g, st, vin, qe, ql, c);
         ++st.level;
-        const int nk = camera_next<N>(sc, st, alive, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next, c);
+        const int nk = camera_next<N>(sc, st, alive, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next,
+                                      cnt_s_next_back, cap, c);
         store_state<N>(states, id, st, nk);
     }
     if (ctr) flush_counters(ctr, K_CAMERA, c);

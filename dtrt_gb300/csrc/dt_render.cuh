@@ -144,7 +144,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         const size_t state_bytes = ((size_t)Bw * sizeof(CamState<N>) + 255) & ~(size_t)255;
         if (wavefront && !(ensure_buffer(&sb.cam_state, &sb.cam_state_bytes, state_bytes + (size_t)Bw * sizeof(VertexIn<N>)) &&
                            ensure_buffer(&sb.cam_q, &sb.cam_q_bytes, (size_t)4 * Bw * sizeof(int)) &&
-                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)2 * (levels + 1) * sizeof(unsigned long long)))) {
+                           ensure_buffer(&sb.cam_cnt, &sb.cam_cnt_bytes, (size_t)3 * (levels + 1) * sizeof(unsigned long long)))) {
             if (s->camera_schedule == DTRT_CAMERA_WAVEFRONT) return DTRT_ERR_CUDA;
             cudaGetLastError();  // AUTO: no room for the path states, run the megakernel
             wavefront = false;
@@ -155,8 +155,10 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
         CamState<N> *states = (CamState<N> *)sb.cam_state;
         VertexIn<N> *vins = (VertexIn<N> *)((char *)sb.cam_state + state_bytes);
         int *qa = (int *)sb.cam_q, *qb = qa + Bw, *qv = qb + Bw, *qs = qv + Bw;
-        // volume and interface vertices queued per level [0, levels]
-        unsigned long long *vcnt = (unsigned long long *)sb.cam_cnt, *scnt = vcnt + (levels + 1);
+        // volume and interface vertices queued per level [0, levels] (interface: pushed from the
+        // front of the queue, scnt, and from its back, sbk)
+        unsigned long long *vcnt = (unsigned long long *)sb.cam_cnt, *scnt = vcnt + (levels + 1),
+                           *sbk = scnt + (levels + 1);
         for (long long b0 = 0; b0 < total; b0 += B) {
             ++batches;
             rp.path_begin = b0;
@@ -166,18 +168,20 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                 // grid-stride launches of a few waves: late levels hold few live paths
                 const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
                 if ((rc = timed(ms_camera, [&] {
-                         cudaMemsetAsync(vcnt, 0, (size_t)2 * (levels + 1) * sizeof(unsigned long long), st);
+                         cudaMemsetAsync(vcnt, 0, (size_t)3 * (levels + 1) * sizeof(unsigned long long), st);
                          // volume / interface queues of level L: (qa, qb) for even L, (qv, qs) for odd L
-                         k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qa, vcnt, qv,
-                                                                                  vcnt + 1, qs, scnt + 1, qe, ql, ctr);
+                         k_cam_start<N><<<blocks(rp.path_count), kBlock, 0, st>>>(
+                             sc, rp, states, vins, qa, vcnt, qv, vcnt + 1, qs, scnt + 1, sbk + 1, Bw, qe, ql, ctr);
                          for (int L = 0; L < levels; ++L) {
                              int *qvl = (L & 1) ? qv : qa, *qsl = (L & 1) ? qs : qb;
                              int *qvn = (L & 1) ? qa : qv, *qsn = (L & 1) ? qb : qs;
-                             k_cam_vertex<N, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qvl, vcnt + L, qvn,
-                                                                          vcnt + L + 1, qsn, scnt + L + 1, qe, ql, ctr);
+                             k_cam_vertex<N, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qvl, vcnt + L, nullptr,
+                                                                          qvn, vcnt + L + 1, qsn, scnt + L + 1,
+                                                                          sbk + L + 1, Bw, qe, ql, ctr);
                              if (L > 0)  // level 0's interface vertices ran in k_cam_start
-                                 k_cam_vertex<N, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qsl, scnt + L, qvn,
-                                                                               vcnt + L + 1, qsn, scnt + L + 1, qe, ql,
+                                 k_cam_vertex<N, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qsl, scnt + L,
+                                                                               sbk + L, qvn, vcnt + L + 1, qsn,
+                                                                               scnt + L + 1, sbk + L + 1, Bw, qe, ql,
                                                                                ctr);
                          }
                          k_cam_accum<N><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, sb.acc1);
@@ -187,7 +191,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                 if (ctr) {
                     // every launched vertex reads and writes its path's state and vertex inputs;
                     // the start writes them once per path, the accumulation reads the sums
-                    std::vector<unsigned long long> lc((size_t)2 * (levels + 1));
+                    std::vector<unsigned long long> lc((size_t)3 * (levels + 1));
                     DT_CK(cudaMemcpyAsync(lc.data(), vcnt, lc.size() * sizeof(unsigned long long),
                                           cudaMemcpyDeviceToHost, st));
                     DT_CK(cudaStreamSynchronize(st));
@@ -198,7 +202,7 @@ int render_n(dtrt_scene *s, const dtrt_render_options *o, float *out, int out_on
                     uint64_t vol = 0, itf = 0;
                     for (int L = 0; L < levels; ++L) {
                         vol += lc[L];
-                        itf += L > 0 ? lc[levels + 1 + L] : 0;
+                        itf += L > 0 ? lc[levels + 1 + L] + lc[2 * (levels + 1) + L] : 0;
                     }
                     state_traffic += 2 * ((sv - si) * vol + sv * itf) + 2 * sizeof(DV<N>) * (uint64_t)rp.path_count;
                 }

@@ -35,7 +35,7 @@ cudaError_t launch_adjoint(const DevScene &sc, const RenderParams &rp, const flo
 size_t AdjWave::bytes(long long cap, int levels) {
     return (size_t)cap * (sizeof(AdjState<1>) + sizeof(VertexIn<1>) + 4 * sizeof(int) + sizeof(float3) +
                           kReplayEvents * sizeof(float3)) +
-           (size_t)4 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 6 arrays
+           (size_t)6 * (levels + 1) * sizeof(unsigned long long) + 2048;  // + 256-byte alignment of 6 arrays
 }
 
 void AdjWave::carve(void *base, long long capacity, int lv) {
@@ -52,7 +52,7 @@ void AdjWave::carve(void *base, long long capacity, int lv) {
     q = (int *)take((size_t)4 * cap * sizeof(int));
     tots = (float3 *)take((size_t)cap * sizeof(float3));
     ev = (float3 *)take((size_t)cap * kReplayEvents * sizeof(float3));
-    cnt = (unsigned long long *)take((size_t)4 * (levels + 1) * sizeof(unsigned long long));
+    cnt = (unsigned long long *)take((size_t)6 * (levels + 1) * sizeof(unsigned long long));
 }
 
 // Wavefront replay of paths [rp.path_begin, +rp.path_count) in chunks of the workspace's
@@ -73,23 +73,26 @@ cudaError_t launch_adjoint_wave(const DevScene &sc, const RenderParams &range, c
         rp.path_begin = range.path_begin + b0;
         rp.path_count = std::min(w.cap, range.path_count - b0);
         const unsigned gw = std::min<unsigned>(blocks(rp.path_count), (unsigned)std::max(1, sms) * 16u);
-        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)4 * (levels + 1) * sizeof(unsigned long long), st);
+        cudaError_t e = cudaMemsetAsync(w.cnt, 0, (size_t)6 * (levels + 1) * sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
         for (int pass = 0; pass < (pass_b ? 2 : 1); ++pass) {
             const bool b = pass == 1;
-            // counts of this pass: volume and interface vertices queued per level [0, levels]
-            unsigned long long *vc = w.cnt + pass * 2 * (levels + 1), *sc_ = vc + (levels + 1);
+            // counts of this pass per level [0, levels]: volume vertices, interface vertices
+            // pushed from the front and from the back of their queue (3 (levels + 1) per pass)
+            unsigned long long *vc = w.cnt + pass * 3 * (levels + 1), *sc_ = vc + (levels + 1);
+            const QueueEnds qx{w.cap, levels + 1};
             // volume / interface queues of level L: (qa, qb) for even L, (qv, qs) for odd L
             k_adj_start<1><<<blocks(rp.path_count), kBlock, 0, st>>>(sc, rp, states, vins, qa, vc, qv, vc + 1, qs,
-                                                                    sc_ + 1, dimg, grad, w.tots, w.ev, b, ctr);
+                                                                    sc_ + 1, dimg, grad, w.tots, w.ev, qx, b, ctr);
             for (int L = 0; L < levels; ++L) {
                 int *qvl = (L & 1) ? qv : qa, *qsl = (L & 1) ? qs : qb;
                 int *qvn = (L & 1) ? qa : qv, *qsn = (L & 1) ? qb : qs;
                 k_adj_vertex<1, true><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qvl, vc + L, qvn, vc + L + 1, qsn,
-                                                            sc_ + L + 1, dimg, grad, w.tots, w.ev, b, ctr);
+                                                            sc_ + L + 1, dimg, grad, w.tots, w.ev, qx, b, ctr);
                 if (L > 0)  // level 0's interface vertices ran in k_adj_start
                     k_adj_vertex<1, false><<<gw, kBlock, 0, st>>>(sc, rp, states, vins, qsl, sc_ + L, qvn, vc + L + 1,
-                                                                 qsn, sc_ + L + 1, dimg, grad, w.tots, w.ev, b, ctr);
+                                                                 qsn, sc_ + L + 1, dimg, grad, w.tots, w.ev, qx, b,
+                                                                 ctr);
             }
             if (pass == 0) k_adj_totals<1><<<blocks(rp.path_count), kBlock, 0, st>>>(rp, states, w.tots, img_acc);
             if (launches) *launches += 2 * levels + (pass == 0 ? 1 : 0);  // start, 2 per level (1 at level 0), totals in pass A

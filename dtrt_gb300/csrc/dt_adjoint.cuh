@@ -370,15 +370,18 @@ DT_D float3 pixel_dldi(const RenderParams &rp, const float *dimg, long long g) {
 template <int N>
 DT_D void replay_next(const DevScene &sc, const RenderParams &rp, AdjState<N> &st, bool alive, bool pass_b,
                       float3 total, float3 gp, AdjCtx &adj, VertexIn<N> *vins, int id, int *qv,
-                      unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, Ctr &c) {
+                      unsigned long long *cnt_v, int *qs, unsigned long long *cnt_s, const QueueEnds &qx, Ctr &c) {
     int kind = 0;
     if (alive && st.mode != 0) {
         VertexIn<N> vin;
         kind = replay_decide<N>(sc, rp, pass_b, total, gp, adj, c, st, vin);
         if (kind) vins[id] = vin;
     }
+    // interface vertices from both ends of their queue by BSDF class, as camera_next
+    const bool back = kind == 2 && interface_back(sc, st.its.shape);
     push_path(qv, cnt_v, id, kind == 1);
-    push_path(qs, cnt_s, id, kind == 2);
+    push_path(qs, cnt_s, id, kind == 2 && !back);
+    push_path_back(qs, qx.cap, cnt_s + qx.back, id, back);
 }
 
 // Path start and level 0 of one pass, as k_cam_start: an interface vertex runs here and
@@ -389,7 +392,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams 
                                                       VertexIn<N> *vins, int *qv0, unsigned long long *cnt_v0,
                                                       int *qv1, unsigned long long *cnt_v1, int *qs1,
                                                       unsigned long long *cnt_s1, const float *dimg, float *grad,
-                                                      const float3 *totals, float3 *evbuf, bool pass_b,
+                                                      const float3 *totals, float3 *evbuf, QueueEnds qx, bool pass_b,
                                                       unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
@@ -419,7 +422,7 @@ __global__ void __launch_bounds__(kBlock) k_adj_start(DevScene sc, RenderParams 
         }
     }
     push_path(qv0, cnt_v0, (int)gi, kind == 1);
-    replay_next<N>(sc, rp, st, next, pass_b, total, gp, adj, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    replay_next<N>(sc, rp, st, next, pass_b, total, gp, adj, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, qx, c);
     if (run) states[gi] = st;
     if (ctr) flush_counters(ctr, K_CAMERA, c);
 }
@@ -432,14 +435,14 @@ __global__ void __launch_bounds__(kBlock) k_adj_vertex(DevScene sc, RenderParams
                                                        const unsigned long long *cnt_in, int *qv_next,
                                                        unsigned long long *cnt_v_next, int *qs_next,
                                                        unsigned long long *cnt_s_next, const float *dimg, float *grad,
-                                                       const float3 *totals, float3 *evbuf, bool pass_b,
+                                                       const float3 *totals, float3 *evbuf, QueueEnds qx, bool pass_b,
                                                        unsigned long long *ctr) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
-    const long long n = (long long)*cnt_in;
+    const long long nf = (long long)*cnt_in, n = nf + (kVolume ? 0 : (long long)cnt_in[qx.back]);
     Ctr c;
     for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
-        const int id = q_in[i];
+        const int id = i < nf ? q_in[i] : q_in[qx.cap - 1 - (i - nf)];
         AdjState<N> st = states[id];
         const VertexIn<N> vin = vins[id];
         const float3 zero = mk(0.f, 0.f, 0.f);
@@ -449,7 +452,8 @@ __global__ void __launch_bounds__(kBlock) k_adj_vertex(DevScene sc, RenderParams
         const bool alive = kVolume ? replay_volume<N>(sc, rp, stack, pass_b, gp, adj, c, ev, st, vin)
                                    : replay_surface<N>(sc, rp, stack, pass_b, gp, adj, c, ev, st, vin);
         ++st.level;
-        replay_next<N>(sc, rp, st, alive, pass_b, total, gp, adj, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next, c);
+        replay_next<N>(sc, rp, st, alive, pass_b, total, gp, adj, vins, id, qv_next, cnt_v_next, qs_next, cnt_s_next,
+                       qx, c);
         states[id] = st;
     }
     if (ctr) flush_counters(ctr, K_CAMERA, c);
@@ -534,7 +538,7 @@ __global__ void __launch_bounds__(kBlock) k_badj_start(BatchWave bw, AdjState<N>
                                                        unsigned long long *cnt_v0, int *qv1,
                                                        unsigned long long *cnt_v1, int *qs1,
                                                        unsigned long long *cnt_s1, const float3 *totals,
-                                                       float3 *evbuf, bool pass_b) {
+                                                       float3 *evbuf, QueueEnds qx, bool pass_b) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
     const long long gi = (long long)blockIdx.x * kBlock + threadIdx.x;
@@ -566,7 +570,8 @@ __global__ void __launch_bounds__(kBlock) k_badj_start(BatchWave bw, AdjState<N>
         }
     }
     push_path(qv0, cnt_v0, (int)gi, kind == 1);
-    replay_next<N>(it.sc, it.rp, st, next, pass_b, total, gp, adj, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, c);
+    replay_next<N>(it.sc, it.rp, st, next, pass_b, total, gp, adj, vins, (int)gi, qv1, cnt_v1, qs1, cnt_s1, qx,
+                   c);
     if (run) states[gi] = st;
 }
 
@@ -575,13 +580,13 @@ __global__ void __launch_bounds__(kBlock) k_badj_vertex(BatchWave bw, AdjState<N
                                                         const int *q_in, const unsigned long long *cnt_in,
                                                         int *qv_next, unsigned long long *cnt_v_next, int *qs_next,
                                                         unsigned long long *cnt_s_next, const float3 *totals,
-                                                        float3 *evbuf, bool pass_b) {
+                                                        float3 *evbuf, QueueEnds qx, bool pass_b) {
     __shared__ int s_stack[kStackDepth * kBlock];
     int *stack = s_stack + threadIdx.x;
-    const long long n = (long long)*cnt_in;
+    const long long nf = (long long)*cnt_in, n = nf + (kVolume ? 0 : (long long)cnt_in[qx.back]);
     Ctr c;
     for (long long i = (long long)blockIdx.x * kBlock + threadIdx.x; i < n; i += (long long)gridDim.x * kBlock) {
-        const int id = q_in[i];
+        const int id = i < nf ? q_in[i] : q_in[qx.cap - 1 - (i - nf)];
         long long g;
         const BatchItemDev &it = batch_item(bw, id, g);
         AdjState<N> st = states[id];
@@ -594,7 +599,7 @@ __global__ void __launch_bounds__(kBlock) k_badj_vertex(BatchWave bw, AdjState<N
                                    : replay_surface<N>(it.sc, it.rp, stack, pass_b, gp, adj, c, ev, st, vin);
         ++st.level;
         replay_next<N>(it.sc, it.rp, st, alive, pass_b, total, gp, adj, vins, id, qv_next, cnt_v_next, qs_next,
-                       cnt_s_next, c);
+                       cnt_s_next, qx, c);
         states[id] = st;
     }
 }

@@ -287,20 +287,22 @@ int enqueue_chunk(dtrt_batch *b, const AdjWave &w, BatchWave bw, cudaStream_t st
     int *qa = w.q, *qb = qa + w.cap, *qv = qb + w.cap, *qs = qv + w.cap;
     {
         const unsigned gw = std::min<unsigned>(blocks(bw.count), (unsigned)std::max(1, b->sms) * 16u);
-        DT_BCK(cudaMemsetAsync(w.cnt, 0, (size_t)4 * (levels + 1) * sizeof(unsigned long long), st));
+        DT_BCK(cudaMemsetAsync(w.cnt, 0, (size_t)6 * (levels + 1) * sizeof(unsigned long long), st));
         for (int pass = 0; pass < (b->any_grad ? 2 : 1); ++pass) {
             const bool pb = pass == 1;
-            unsigned long long *vc = w.cnt + pass * 2 * (levels + 1), *scn = vc + (levels + 1);
+            // per level: volume, interface front-end and back-end counts (as launch_adjoint_wave)
+            unsigned long long *vc = w.cnt + pass * 3 * (levels + 1), *scn = vc + (levels + 1);
+            const QueueEnds qx{w.cap, levels + 1};
             k_badj_start<1><<<blocks(bw.count), kBlock, 0, st>>>(bw, states, vins, qa, vc, qv, vc + 1, qs, scn + 1,
-                                                                w.tots, w.ev, pb);
+                                                                w.tots, w.ev, qx, pb);
             for (int L = 0; L < levels; ++L) {
                 int *qvl = (L & 1) ? qv : qa, *qsl = (L & 1) ? qs : qb;
                 int *qvn = (L & 1) ? qa : qv, *qsn = (L & 1) ? qb : qs;
                 k_badj_vertex<1, true><<<gw, kBlock, 0, st>>>(bw, states, vins, qvl, vc + L, qvn, vc + L + 1, qsn,
-                                                             scn + L + 1, w.tots, w.ev, pb);
+                                                             scn + L + 1, w.tots, w.ev, qx, pb);
                 if (L > 0)
                     k_badj_vertex<1, false><<<gw, kBlock, 0, st>>>(bw, states, vins, qsl, scn + L, qvn, vc + L + 1,
-                                                                  qsn, scn + L + 1, w.tots, w.ev, pb);
+                                                                  qsn, scn + L + 1, w.tots, w.ev, qx, pb);
             }
             if (pass == 0) k_badj_totals<1><<<blocks(bw.count), kBlock, 0, st>>>(bw, states, w.tots);
         }

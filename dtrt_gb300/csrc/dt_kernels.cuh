@@ -490,6 +490,13 @@ DT_D void push_path(int *q, unsigned long long *count, int id, bool pred) {
     if (pred) q[base + __popc(m & ((1u << lane) - 1u))] = id;  // at most one push per path and level
 }
 
+// A level's two-ended interface queue: `cap` slots, and the count of the back end `back`
+// entries after the count of the front end
+struct QueueEnds {
+    long long cap;
+    int back;
+};
+
 // push from the back of a queue of `cap` slots: entry k at q[cap - 1 - k]
 DT_D void push_path_back(int *q, long long cap, unsigned long long *count, int id, bool pred) {
     const unsigned act = __activemask();

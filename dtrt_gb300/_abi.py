@@ -154,7 +154,7 @@ BATCH_AUTOTUNE, BATCH_GRAPH, BATCH_TUNE_FULL, BATCH_WAVEFRONT = 1, 2, 4, 8
 
 class BatchItem(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("opts", RenderOptions), ("d_image", ctypes.c_void_p),
-                ("image", ctypes.c_void_p), ("d_density", ctypes.c_void_p)]
+                ("image", ctypes.c_void_p), ("d_density", ctypes.c_void_p), ("d_vertices", ctypes.c_void_p)]
 
 
 class BatchStats(ctypes.Structure):
@@ -167,7 +167,7 @@ class BatchStats(ctypes.Structure):
         ("trial_ms", ctypes.c_float * BATCH_MAX_TRIALS), ("tune_sample_stride", ctypes.c_int64),
         ("full_ms", ctypes.c_float * 4),
         ("item_ms_estimate", ctypes.c_double * BATCH_MAX_ITEMS), ("order", ctypes.c_int * BATCH_MAX_ITEMS),
-        ("full_ms_wavefront", ctypes.c_float), ("wave_capacity", ctypes.c_int64),
+        ("full_ms_wavefront", ctypes.c_float), ("wave_capacity", ctypes.c_int64), ("vertex_items", ctypes.c_int),
     ]
 
     def as_dict(self):
@@ -189,7 +189,7 @@ class BatchStats(ctypes.Structure):
                 "full_size_ms": {"persistent": self.full_ms[0], "per_item_1": self.full_ms[1],
                                  "per_item_2": self.full_ms[2], "per_item_4": self.full_ms[3],
                                  "wavefront": self.full_ms_wavefront},
-                "wave_capacity": self.wave_capacity,
+                "wave_capacity": self.wave_capacity, "vertex_items": self.vertex_items,
                 "item_ms_estimate": list(self.item_ms_estimate[:min(n, BATCH_MAX_ITEMS)]),
                 "order": list(self.order[:min(n, BATCH_MAX_ITEMS)])}
 

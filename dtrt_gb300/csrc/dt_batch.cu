@@ -117,6 +117,7 @@ struct dtrt_batch {
     unsigned long long *d_next = nullptr;
     unsigned int *d_err = nullptr;
     std::vector<double *> img_acc;
+    std::vector<int> vert_items;  // items with d_vertices: the vertex replay after the captured launch
     // launch shape
     int grid = 0, chunk = 128, n_img = 0;
     long long total_chunks = 0, total_pix = 0;
@@ -616,7 +617,7 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
     DT_BCK(cudaMalloc(&b->d_err, 4));
     for (int i = 0; i < n; ++i) {
         const dtrt_batch_item &it = items[i];
-        if (!it.scene || it.opts.spp < 0 || it.opts.max_bounces < 0 || (!it.image && !it.d_density)) {
+        if (!it.scene || it.opts.spp < 0 || it.opts.max_bounces < 0 || (!it.image && !it.d_density && !it.d_vertices)) {
             set_last_error("batch item " + std::to_string(i) + ": needs a scene, spp/max_bounces >= 0 and an output");
             return DTRT_ERR_INVALID;
         }
@@ -624,10 +625,17 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
             set_last_error("batch items must live on the current device");
             return DTRT_ERR_INVALID;
         }
-        if (it.d_density && !it.d_image) {
-            set_last_error("batch item " + std::to_string(i) + ": d_density needs d_image");
+        if ((it.d_density || it.d_vertices) && !it.d_image) {
+            set_last_error("batch item " + std::to_string(i) + ": d_density and d_vertices need d_image");
             return DTRT_ERR_INVALID;
         }
+        if (it.d_vertices && it.d_density) {
+            set_last_error("batch item " + std::to_string(i) + ": d_vertices takes no d_density");
+            return DTRT_ERR_INVALID;
+        }
+        // a vertex item has no paths in the batch's launch: the vertex replay renders it
+        const bool vertex_item = it.d_vertices != nullptr;
+        if (vertex_item) b->vert_items.push_back(i);
         DevScene sc = it.scene->dev;
         sc.vert_der = nullptr;
         sc.face_n_der = nullptr;
@@ -651,7 +659,7 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
         rp.crop_x = cropped ? cam.crop_x : 0;
         rp.crop_y = cropped ? cam.crop_y : 0;
         rp.npix = rp.out_w * rp.out_h;
-        const long long paths = (long long)rp.npix * std::max(0, it.opts.spp);
+        const long long paths = vertex_item ? 0 : (long long)rp.npix * std::max(0, it.opts.spp);
         rp.path_begin = 0;
         rp.path_count = paths;
         BatchItemDev d{};
@@ -661,7 +669,7 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
         d.grad = (it.d_density && it.scene->density_voxels > 0) ? it.d_density : nullptr;
         d.img_acc = nullptr;
         double *acc = nullptr;
-        if (it.image) {
+        if (it.image && !vertex_item) {
             DT_BCK(cudaMalloc(&acc, (size_t)rp.npix * 3 * 8));
             d.img_acc = acc;
         }
@@ -679,7 +687,7 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
     std::vector<BatchImageDev> imgs;
     long long pix = 0;
     for (int i = 0; i < n; ++i)
-        if (items[i].image) {
+        if (items[i].image && b->img_acc[i]) {
             imgs.push_back({b->img_acc[i], items[i].image, pix});
             pix += (long long)b->npix[i];
         }
@@ -769,6 +777,7 @@ int dtrt_batch_create(const dtrt_batch_item *items, int n, unsigned flags, void 
     b->stats.wave_capacity = b->bw_mem ? b->bw.cap : 0;
     for (int i = 0; i < n && i < DTRT_BATCH_MAX_ITEMS; ++i) b->stats.order[i] = b->order[i];
     b->stats.num_items = n;
+    b->stats.vertex_items = (int)b->vert_items.size();
     long long tp = 0;
     for (long long p : b->paths) tp += p;
     b->stats.total_paths = (uint64_t)tp;
@@ -803,6 +812,13 @@ int dtrt_batch_launch(dtrt_batch *b, void *stream) {
             k_batch_image<<<(unsigned)((b->total_pix + 255) / 256), 256, 0, st>>>(b->d_imgs, b->n_img, b->total_pix);
             DT_BCK(cudaGetLastError());
         }
+    }
+    // vertex items: the vertex-position replay of each (its chunking reads queue counts on
+    // the host, so it runs outside the captured graph), on the same stream
+    for (int i : b->vert_items) {
+        const dtrt_batch_item &it = b->items[i];
+        const int rc = render_vertex_adjoint(it.scene, &it.opts, it.d_image, it.image, it.d_vertices, 1, st);
+        if (rc) return rc;
     }
     unsigned int herr = 0;
     DT_BCK(cudaMemcpyAsync(&herr, b->d_err, 4, cudaMemcpyDeviceToHost, st));

@@ -389,9 +389,14 @@ int dtrt_render_adjoint(dtrt_scene *scene, const dtrt_render_options *opts, cons
 typedef struct {
     dtrt_scene *scene;
     dtrt_render_options opts;  /* seed, spp, max_bounces, sppe (< 0: no pixel jitter), mode */
-    const float *d_image;      /* NULL or device [H][W][3] dL/dI (needed with d_density) */
+    const float *d_image;      /* NULL or device [H][W][3] dL/dI (needed with d_density / d_vertices) */
     float *image;              /* NULL or device [H][W][3] */
     float *d_density;          /* NULL or device [density_voxels] */
+    float *d_vertices;         /* NULL or device [vertices][3]: the vertex-position adjoint of a
+                                  surface scene (dtrt_render_adjoint's contract). Such an item
+                                  (with its image) is rendered after the batch's captured launch
+                                  by the vertex replay, whose chunking waits on the host, and it
+                                  takes no other output (d_density must be NULL). */
 } dtrt_batch_item;
 
 #define DTRT_BATCH_AUTOTUNE 1u /* measure item costs and pick item order and chunk size */
@@ -423,6 +428,7 @@ typedef struct {
     int order[DTRT_BATCH_MAX_ITEMS];
     float full_ms_wavefront;        /* DTRT_BATCH_TUNE_FULL: the batch wavefront (-1: not confirmed) */
     int64_t wave_capacity;          /* paths per workspace of the batch wavefront (0: not available) */
+    int vertex_items;               /* items with d_vertices (rendered after the captured launch) */
 } dtrt_batch_stats;
 
 typedef struct dtrt_batch dtrt_batch;

@@ -208,19 +208,21 @@ class Batch:
     """Many scenes rendered together (dtrt_batch_create / _launch / _destroy): a persistent
     launch, per-item launches over streams, or one replay wavefront over all items.
 
-    items: list of (NativeScene, options, d_image_ptr, image_ptr, d_density_ptr) with
-    device pointers as ints (0 = none). The scenes and buffers must outlive the batch."""
+    items: list of (NativeScene, options, d_image_ptr, image_ptr, d_density_ptr[, d_vertices_ptr])
+    with device pointers as ints (0 = none). The scenes and buffers must outlive the batch."""
 
     def __init__(self, items, autotune=True, graph=True, stream=None, tune_full=False, wavefront=False):
         self.lib = _abi.load()
         self.scenes = [it[0] for it in items]  # keep the scenes alive
         arr = (_abi.BatchItem * len(items))()
-        for i, (sc, opts, dimg, img, dden) in enumerate(items):
+        for i, item in enumerate(items):
+            sc, opts, dimg, img, dden = item[:5]
             arr[i].scene = sc.handle.value
             arr[i].opts = opts
             arr[i].d_image = dimg or None
             arr[i].image = img or None
             arr[i].d_density = dden or None
+            arr[i].d_vertices = (item[5] if len(item) > 5 else 0) or None
         flags = (_abi.BATCH_AUTOTUNE if autotune else 0) | (_abi.BATCH_GRAPH if graph else 0) | \
             (_abi.BATCH_TUNE_FULL if tune_full else 0) | (_abi.BATCH_WAVEFRONT if wavefront else 0)
         h = ctypes.c_void_p()
